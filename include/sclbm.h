@@ -1,0 +1,163 @@
+/*
+ * sclbm.h -- C ABI of the GB300-native Shan-Chen multiphase LBM time step.
+ *
+ * One handle = one periodic lattice resident in HBM (populations stored SoA,
+ * q-major, x fastest), stepped by hand-written sm_103a kernels.  Every call
+ * returns an int status (SCLBM_OK == 0) and never aborts; host buffers are
+ * owned by the caller, device state by the handle.  Calls on one handle are
+ * not thread-safe; distinct handles are independent.
+ *
+ * The entry points replace the generated kernels and the per-step dispatch of
+ * the reference (lullimat/idea.deploy, package idpy):
+ *
+ *   sclbm_create            ShanChenMultiPhase.__init__ / SetupRoot / InitVars /
+ *                           InitMemory          idpy/LBM/MultiPhase.py:141-155,1941-2169
+ *   sclbm_set_density/_velocity
+ *                           sims_idpy_memory['n'|'u'].H2D   idpy/IdpyCode/IdpyMemory.py:343-425
+ *   sclbm_init_populations  InitPopulations + K_InitPopulationsMeta
+ *                                           idpy/LBM/MultiPhase.py:1664-1688,
+ *                                           idpy/LBM/LBMKernelsMeta.py:282-387
+ *   sclbm_init_radial / _flat / _single_flat / _cylinder
+ *                           InitRadialInterface, InitFlatInterface, ...
+ *                                           idpy/LBM/MultiPhase.py:1771-1937,
+ *                                           idpy/LBM/MultiPhaseKernels.py:605-777
+ *   sclbm_step              MainLoop / MainLoopMRT step loop (K_ComputeDensityPsiMeta +
+ *                           K_ForceCollideStreamSCMP[_MRT]Meta + M_SwapPop per step)
+ *                                           idpy/LBM/MultiPhase.py:1015-1097,1311-1402,
+ *                                           idpy/IdpyCode/IdpyCode.py:1715-1851
+ *   sclbm_compute_moments   ComputeMomentsMeta (+ K_ComputeVelocityAfterForceSCMPMeta)
+ *                                           idpy/LBM/MultiPhase.py:1565-1661
+ *   sclbm_get_density/_velocity/_populations
+ *                           GetDensityField / GetVelocityField / GetPopulations
+ *                                           idpy/LBM/LBM.py:634-667
+ *   sclbm_check_u           CheckUConvergenceSCMP + K_CheckUMeta
+ *                                           idpy/LBM/MultiPhaseLoopChecks.py:96-163,
+ *                                           idpy/LBM/LBMKernelsMeta.py:389-498
+ *   sclbm_center_of_mass    ComputeCenterOfMass  idpy/LBM/MultiPhase.py:108-137
+ *   sclbm_density_at        K_NInNOut (used by DeltaPLaplace) idpy/LBM/LBMKernels.py:506-523
+ *   sclbm_destroy           End()            idpy/LBM/MultiPhase.py:2171-2175
+ */
+#ifndef SCLBM_H
+#define SCLBM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define SCLBM_OK              0
+#define SCLBM_ERR_ARG         1   /* invalid argument (null pointer, bad size, ...) */
+#define SCLBM_ERR_UNSUPPORTED 2   /* lattice / stencil / option not built in */
+#define SCLBM_ERR_CUDA        3   /* a CUDA runtime call failed */
+#define SCLBM_ERR_STATE       4   /* call out of order (e.g. step before init) */
+#define SCLBM_ERR_NOMEM       5   /* device allocation failed */
+#define SCLBM_ERR_NODEVICE    6   /* no usable sm_100-family device */
+
+/* pseudopotential psi(n) */
+#define SCLBM_PSI_EXP_INV       0  /* psi = exp(-1/n)   ('exp(-1./ln_0)')     */
+#define SCLBM_PSI_ONE_MINUS_EXP 1  /* psi = 1 - exp(-n) ('(1. - exp(-ln_0))') */
+#define SCLBM_PSI_IDENTITY      2  /* psi = n           ('ln_0')              */
+
+/* collision */
+#define SCLBM_COLL_BGK 0           /* BGK + Guo forcing, omega = 1/tau */
+#define SCLBM_COLL_MRT 1           /* MRT + Guo forcing in the W-orthogonal Hermite basis */
+
+/* storage / arithmetic precision of the populations */
+#define SCLBM_FP64         0       /* plain FP64, as the reference */
+#define SCLBM_FP32_SHIFTED 1       /* FP32 deviations f_q - w_q*rho0, FP64 reductions */
+
+/* coefficient literals of the expanded collision */
+#define SCLBM_LIT_ROUND15 0        /* 15-significant-digit literals, as sympy evalf() emits */
+#define SCLBM_LIT_EXACT   1        /* exact coefficients rounded once to double */
+
+typedef struct sclbm_sim sclbm_sim;
+
+typedef struct sclbm_params {
+    int dim;                   /* 2 or 3 */
+    int sizes[3];              /* lattice sizes, x first (unused entries ignored) */
+    int q;                     /* number of lattice velocities (9: D2Q9, 19: D3Q19) */
+    const int *xi;             /* q*dim lattice velocities, in the reference's order */
+    const double *w;           /* q lattice weights */
+    double c2;                 /* squared sound speed (1/3) */
+    int qe;                    /* force-stencil vectors */
+    const int *e;              /* qe*dim force-stencil vectors (E4/E6/E8 tables) */
+    const double *we;          /* qe force-stencil weights */
+    double sc_g;               /* Shan-Chen coupling G */
+    int psi_kind;              /* SCLBM_PSI_* */
+    int collision;             /* SCLBM_COLL_* */
+    double tau;                /* BGK relaxation time (omega = 1/tau) */
+    const double *mrt_s;       /* MRT: q*q relaxation matrix S in the moment basis
+                                  (row-major; a diagonal S holds the per-moment rates) */
+    int precision;             /* SCLBM_FP64 / SCLBM_FP32_SHIFTED */
+    double rho0;               /* FP32_SHIFTED: reference density of the shift */
+    int literals;              /* SCLBM_LIT_* (FP64 path) */
+    int device;                /* CUDA device ordinal */
+} sclbm_params;
+
+/* library */
+const char *sclbm_version(void);
+const char *sclbm_status_string(int status);
+/* message of the last failed call on this thread (empty if none) */
+const char *sclbm_last_error(void);
+
+/* lifetime */
+int sclbm_create(const sclbm_params *p, sclbm_sim **out);
+int sclbm_destroy(sclbm_sim *s);
+
+/* lattice volume and the footprint of the handle in device memory */
+int sclbm_info(const sclbm_sim *s, int64_t *volume, int64_t *device_bytes);
+
+/* fields; host arrays are FP64, x fastest; u as dim planes of volume values */
+int sclbm_set_density(sclbm_sim *s, const double *n);
+int sclbm_set_velocity(sclbm_sim *s, const double *u);
+int sclbm_get_density(sclbm_sim *s, double *n);
+int sclbm_get_velocity(sclbm_sim *s, double *u);
+/* populations as q planes of volume values (f_q, not the FP32 deviations) */
+int sclbm_get_populations(sclbm_sim *s, double *pop);
+int sclbm_set_populations(sclbm_sim *s, const double *pop);
+
+/* initialisation */
+int sclbm_init_populations(sclbm_sim *s);
+int sclbm_init_radial(sclbm_sim *s, double n_g, double n_l, double R, int full_flag);
+int sclbm_init_flat(sclbm_sim *s, double n_g, double n_l, double width, int direction,
+                    int full_flag);
+int sclbm_init_single_flat(sclbm_sim *s, double n_g, double n_l, int direction, int full_flag);
+int sclbm_init_cylinder(sclbm_sim *s, double n_g, double n_l, double R, int direction,
+                        int full_flag);
+
+/* time stepping: enqueue nsteps steps on the handle's stream (returns without
+ * waiting); sclbm_sync waits for everything enqueued on the handle */
+int sclbm_step(sclbm_sim *s, int64_t nsteps);
+int sclbm_sync(sclbm_sim *s);
+/* as sclbm_step, bracketed by CUDA events on the handle's stream; waits and
+ * returns the elapsed device time in milliseconds */
+int sclbm_step_timed(sclbm_sim *s, int64_t nsteps, double *ms);
+/* per-kernel device time of one step, averaged over nsteps (ms[0]: density+psi
+ * pass, ms[1]: fused force+collide+stream pass); kernels are launched one by
+ * one, each bracketed by events */
+int sclbm_profile_step(sclbm_sim *s, int64_t nsteps, double *ms, int nms);
+/* count of kernels launched by sclbm_step per lattice step */
+int sclbm_kernels_per_step(const sclbm_sim *s, int *count);
+
+/* observables */
+int sclbm_compute_moments(sclbm_sim *s);
+/* sum of all populations (FP64 accumulation) and total momentum sum_q xi_q f_q */
+int sclbm_reductions(sclbm_sim *s, double *mass, double *momentum);
+/* CheckUConvergenceSCMP on the last compute_moments velocity:
+ * u_conv = sum_cells sum_d |u - u_old| / V, max_u = sqrt(max |u|^2 / c2); then
+ * u_old = u.  The first call compares against zero, as the reference does. */
+int sclbm_check_u(sclbm_sim *s, double *u_conv, double *max_u);
+/* mass and centre of mass sum(n x_d)/sum(n) from the density field */
+int sclbm_center_of_mass(sclbm_sim *s, double *mass, double *cm);
+/* density at count linear cell indices */
+int sclbm_density_at(sclbm_sim *s, const int64_t *idx, int count, double *out);
+/* 1 if every density value is finite, else 0 (max |n| also returned) */
+int sclbm_density_finite(sclbm_sim *s, int *finite, double *max_abs);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SCLBM_H */

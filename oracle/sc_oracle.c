@@ -1,0 +1,251 @@
+/*
+ * CPU oracle for the Shan-Chen multiphase LBM time step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This file restates, in plain C, the arithmetic of
+ * the reference's CTypes FP64 path (lullimat/idea.deploy, package idpy) so the
+ * CUDA path can be checked against it.  Only tests/, the smoke check and the
+ * CPU-baseline leg of bench.py may load it; the product never does.
+ *
+ * Layout follows the reference's 'cpu' ordering: pop[q + g*Q], u[d + g*D],
+ * g = x + L0*(y + L1*z) (idpy/LBM/LBM.py:529-537).
+ *
+ * The collision is driven by term tables built in oracle.py: for every
+ * population q a list of terms ((coef * x1) * x2) * x3 summed left to right,
+ * where x_i index the per-cell value vector
+ *      v = [n, u_0..u_{D-1}, F_0..F_{D-1}, f_0..f_{Q-1}].
+ * That is exactly how the generated C of the reference evaluates each
+ * post-collision population (idpy/LBM/Collisions.py:251-316 emits the
+ * expanded sympy expression; terms appear in sympy's print order), so with
+ * the reference's own literals the oracle is bit-identical to it.
+ *
+ * Reference kernels restated here:
+ *   K_ComputeDensityPsiMeta               idpy/LBM/MultiPhaseKernelsMeta.py:107-167
+ *   K_ForceCollideStreamSCMPMeta          idpy/LBM/MultiPhaseKernelsMeta.py:169-345
+ *   K_ForceCollideStreamSCMP_MRTMeta      idpy/LBM/MultiPhaseKernelsMeta.py:891-1075
+ *   K_ComputeVelocityAfterForceSCMPMeta   idpy/LBM/MultiPhaseKernelsMeta.py:1077-1219
+ *   K_InitPopulationsMeta                 idpy/LBM/LBMKernelsMeta.py:282-387
+ *   SC force (gradient) codegen           idpy/LBM/IDShanChenForce.py:44-116,
+ *                                         idpy/IdpyStencils/IdpyStencils.py:1431-1596
+ *   periodic neighbour wrap               idpy/IdpyCode/IdpyUnroll.py:37-48
+ */
+#include <math.h>
+#include <stddef.h>
+#include <stdint.h>
+#include <stdlib.h>
+
+#define ORC_MAXQ 27
+#define ORC_MAXT 64
+
+enum { ORC_PSI_EXP_INV = 0, ORC_PSI_ONE_MINUS_EXP = 1, ORC_PSI_IDENTITY = 2 };
+
+typedef struct {
+    int dim;          /* 2 or 3 */
+    int L[3];         /* sizes, x first */
+    int Q;            /* lattice populations */
+    int QE;           /* force-stencil vectors */
+    const int *xi;    /* Q*dim lattice velocities */
+    const int *e;     /* QE*dim force-stencil vectors */
+    const double *we; /* QE force-stencil weights (double, as the caller gives them) */
+    double G;         /* Shan-Chen coupling */
+    int psi_kind;
+    /* collision terms: for q, terms [t_off[q], t_off[q+1]) */
+    const int *t_off;      /* Q+1 */
+    const double *t_coef;  /* T */
+    const int *t_nf;       /* T: factors (0..3) */
+    const int *t_fid;      /* 3*T factor ids into v */
+    /* velocity sums, per d: signed population list in order */
+    const int *v_off;      /* D+1 */
+    const int *v_pop;      /* population index */
+    const int *v_sign;     /* +1 / -1 */
+    /* density sum order */
+    const int *n_order;    /* Q */
+} orc_cfg;
+
+static inline int wrap(int x, int L) {
+    /* branch-free periodic wrap for |offset| < L, as in the reference macros */
+    if (x >= L) return x - L;
+    if (x < 0) return x + L;
+    return x;
+}
+
+static inline double psi_of(int kind, double n) {
+    switch (kind) {
+    case ORC_PSI_EXP_INV: return exp(-1. / n);
+    case ORC_PSI_ONE_MINUS_EXP: return (1. - exp(-n));
+    default: return n;
+    }
+}
+
+static inline void coords(const orc_cfg *c, long g, int *x) {
+    x[0] = (int)(g % c->L[0]);
+    if (c->dim == 2) {
+        x[1] = (int)(g / c->L[0]);
+        x[2] = 0;
+    } else {
+        x[1] = (int)((g / c->L[0]) % c->L[1]);
+        x[2] = (int)(g / ((long)c->L[0] * c->L[1]));
+    }
+}
+
+static inline long index_of(const orc_cfg *c, const int *x) {
+    long g = x[0];
+    g += (long)c->L[0] * x[1];
+    if (c->dim == 3) g += (long)c->L[0] * c->L[1] * x[2];
+    return g;
+}
+
+static inline long neighbour(const orc_cfg *c, const int *x, const int *off) {
+    int y[3] = {0, 0, 0};
+    for (int d = 0; d < c->dim; d++) y[d] = wrap(x[d] + off[d], c->L[d]);
+    return index_of(c, y);
+}
+
+static long volume(const orc_cfg *c) {
+    long V = 1;
+    for (int d = 0; d < c->dim; d++) V *= c->L[d];
+    return V;
+}
+
+/* n = sum_q f_q (reference print order), psi = psi(n) */
+int orc_density_psi(const orc_cfg *c, const double *pop, double *n, double *psi) {
+    const long V = volume(c);
+    const int Q = c->Q;
+    for (long g = 0; g < V; g++) {
+        const double *f = pop + g * Q;
+        double s = f[c->n_order[0]];
+        for (int i = 1; i < Q; i++) s = s + f[c->n_order[i]];
+        psi[g] = psi_of(c->psi_kind, s);
+        n[g] = s;
+    }
+    return 0;
+}
+
+/* F_d = -G psi(x) sum_a w_a e_{a,d} psi(x+e_a), accumulated as the reference does */
+static void sc_force(const orc_cfg *c, const double *psi, long g, const int *x, double *F) {
+    double dp[3] = {0., 0., 0.};
+    for (int a = 0; a < c->QE; a++) {
+        const int *e = c->e + a * c->dim;
+        const long nb = neighbour(c, x, e);
+        const double p = psi[nb];
+        for (int d = 0; d < c->dim; d++) {
+            if (e[d] == 0) continue;
+            const double w = (double)abs(e[d]) * c->we[a];
+            if (e[d] > 0) dp[d] += w * p;
+            else dp[d] -= w * p;
+        }
+    }
+    const double s = -c->G * psi[g];
+    for (int d = 0; d < c->dim; d++) F[d] = dp[d] * s;
+}
+
+/* u_d = (sum_q xi_{q,d} f_q)/n, then u_d += 0.5*F_d/n (Guo shift) */
+static void velocity(const orc_cfg *c, const double *f, double n, const double *F, double *u) {
+    for (int d = 0; d < c->dim; d++) {
+        double s = 0.;
+        int first = 1;
+        for (int k = c->v_off[d]; k < c->v_off[d + 1]; k++) {
+            const double t = c->v_sign[k] > 0 ? f[c->v_pop[k]] : -f[c->v_pop[k]];
+            if (first) { s = t; first = 0; }
+            else s = s + t;
+        }
+        u[d] = s / n;
+        u[d] += 0.5 * F[d] / n;
+    }
+}
+
+static inline double eval_terms(const orc_cfg *c, int q, const double *v) {
+    double acc = 0.;
+    int first = 1;
+    for (int t = c->t_off[q]; t < c->t_off[q + 1]; t++) {
+        double p = c->t_coef[t];
+        const int nf = c->t_nf[t];
+        for (int k = 0; k < nf; k++) p = p * v[c->t_fid[3 * t + k]];
+        if (first) { acc = p; first = 0; }
+        else acc = acc + p;
+    }
+    return acc;
+}
+
+/* One fused force + collision + push-stream pass: pop -> pop_swap */
+int orc_force_collide_stream(const orc_cfg *c, const double *pop, const double *n,
+                             const double *psi, double *pop_swap) {
+    const long V = volume(c);
+    const int Q = c->Q, D = c->dim;
+    double v[1 + 6 + ORC_MAXQ];
+    for (long g = 0; g < V; g++) {
+        int x[3];
+        coords(c, g, x);
+        double F[3];
+        sc_force(c, psi, g, x, F);
+        const double *f = pop + g * Q;
+        double u[3];
+        velocity(c, f, n[g], F, u);
+        v[0] = n[g];
+        for (int d = 0; d < D; d++) { v[1 + d] = u[d]; v[1 + D + d] = F[d]; }
+        for (int q = 0; q < Q; q++) v[1 + 2 * D + q] = f[q];
+        for (int q = 0; q < Q; q++) {
+            const long dst = neighbour(c, x, c->xi + q * D);
+            pop_swap[q + dst * Q] = eval_terms(c, q, v);
+        }
+    }
+    return 0;
+}
+
+/* ComputeMomentsMeta second kernel: writes n (unchanged) and the shifted u */
+int orc_velocity_after_force(const orc_cfg *c, const double *pop, const double *n,
+                             const double *psi, double *u_out) {
+    const long V = volume(c);
+    const int Q = c->Q, D = c->dim;
+    for (long g = 0; g < V; g++) {
+        int x[3];
+        coords(c, g, x);
+        double F[3], u[3];
+        sc_force(c, psi, g, x, F);
+        velocity(c, pop + g * Q, n[g], F, u);
+        for (int d = 0; d < D; d++) u_out[d + g * D] = u[d];
+    }
+    return 0;
+}
+
+/* Equilibrium populations from (n, u): same term tables, products formed first
+ * (the reference precomputes n*u_a and n*u_a*u_b, LBMKernelsMeta.py:282-387). */
+int orc_init_populations(const orc_cfg *c, const double *n, const double *u, double *pop) {
+    const long V = volume(c);
+    const int Q = c->Q, D = c->dim;
+    double v[1 + 6 + ORC_MAXQ];
+    for (long g = 0; g < V; g++) {
+        v[0] = n[g];
+        for (int d = 0; d < D; d++) { v[1 + d] = u[d + g * D]; v[1 + D + d] = 0.; }
+        for (int q = 0; q < Q; q++) {
+            double acc = 0.;
+            int first = 1;
+            for (int t = c->t_off[q]; t < c->t_off[q + 1]; t++) {
+                const int nf = c->t_nf[t];
+                double p = 1.;
+                if (nf > 0) {
+                    p = v[c->t_fid[3 * t]];
+                    for (int k = 1; k < nf; k++) p = p * v[c->t_fid[3 * t + k]];
+                }
+                p = c->t_coef[t] * p;
+                if (first) { acc = p; first = 0; }
+                else acc = acc + p;
+            }
+            pop[q + g * Q] = acc;
+        }
+    }
+    return 0;
+}
+
+/* nsteps of MainLoop: density/psi, fused step, swap (IdpyLoop.Run).  On return
+ * the current populations are in *pop_a (buffers are swapped as needed). */
+int orc_run(const orc_cfg *c, double *pop_a, double *pop_b, double *n, double *psi,
+            int nsteps, int *swapped) {
+    double *cur = pop_a, *nxt = pop_b;
+    for (int s = 0; s < nsteps; s++) {
+        orc_density_psi(c, cur, n, psi);
+        orc_force_collide_stream(c, cur, n, psi, nxt);
+        double *t = cur; cur = nxt; nxt = t;
+    }
+    *swapped = (cur != pop_a);
+    return 0;
+}
