@@ -1,0 +1,404 @@
+#!/usr/bin/env python
+"""Benchmark: D3Q19 Shan-Chen time step, MLUPS and fraction of the HBM roofline.
+
+Workload (one "step" = one lattice time step over the whole box): D3Q19, E6
+isotropic force stencil, MRT collision with every relaxation rate 1.0, Guo
+forcing, psi = exp(-1/rho), G = -5.0, 256^3 periodic box, a spherical droplet
+of radius 40 (tanh width 2, rho_l = 2.2, rho_g = 0.15, 1e-4 seeded noise),
+populations stored as FP32 deviations from w_q*rho0.  The FP64 path on the
+same workload is reported beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+``--impl reference`` times the reference's own CPU implementation of the
+step (its generated CTypes kernels, built from oracle/_ref) on the host cores,
+one independent sample box per thread.  Multi-GPU: replicas only (every rank
+runs its own box; no data exchange), launched one rank per GPU by torchrun.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, 'idea.deploy_gb300')):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+METRIC = 'D3Q19 Shan-Chen MLUPS (E6 stencil, MRT, FP32-shifted populations)'
+BOX = (256, 256, 256)
+R, RHO_L, RHO_G, WIDTH, SEED, G = 40.0, 2.2, 0.15, 2.0, 1234, -5.0
+Q = 19
+WORKLOAD = ('D3Q19 E6 MRT (all rates 1.0) + Guo, psi=exp(-1/rho), G=-5.0, 256^3 periodic, '
+            'droplet R=40 tanh width 2, rho_l=2.2 rho_g=0.15, 1e-4 seeded noise')
+
+
+def dist_env():
+    ws = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return ws, rank, local
+
+
+class Dist:
+    """Barrier and max-over-ranks (torch.distributed only when WORLD_SIZE > 1)."""
+
+    def __init__(self):
+        self.ws, self.rank, self.local = dist_env()
+        self.pg = None
+        if self.ws > 1:
+            import torch
+            import torch.distributed as tdist
+            torch.cuda.set_device(self.local)
+            tdist.init_process_group('nccl')
+            self.torch, self.tdist = torch, tdist
+
+    def barrier(self):
+        if self.ws > 1:
+            self.tdist.barrier()
+
+    def max(self, x):
+        if self.ws == 1:
+            return x
+        t = self.torch.tensor([float(x)], device='cuda')
+        self.tdist.all_reduce(t, op=self.tdist.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.tdist.destroy_process_group()
+
+
+# ----------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ----------------------------------------------------------------------------
+class Clocks:
+    Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+         'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+         'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu):
+        self.gpu, self.p, self.lines = gpu, None, []
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(['nvidia-smi', '-i', str(self.gpu), '--query-gpu=' + self.Q,
+                                       '--format=csv,noheader,nounits', '-lms', '100'],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            out, _ = self.p.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+            out, _ = self.p.communicate()
+        rows = []
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(',')]
+            if len(f) >= 9:
+                rows.append(f)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace('.', '').isdigit()]
+        reasons = set()
+        for r in rows:
+            for name, v in zip(['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap'],
+                               r[5:9]):
+                if v.strip().lower() in ('active', '1', 'yes'):
+                    reasons.add(name)
+        return {'sm_mhz': float(np.median(sm)) if sm else None,
+                'sm_max_mhz': float(rows[0][2]) if rows[0][2].replace('.', '').isdigit() else None,
+                'power_w_max': max(float(r[3]) for r in rows if r[3].replace('.', '').isdigit()),
+                'samples': len(rows), 'reasons': sorted(reasons)}
+
+
+# ----------------------------------------------------------------------------
+# CPU: the reference's generated kernels (oracle/_ref) or the oracle port
+# ----------------------------------------------------------------------------
+def _ref_kernels(tag):
+    import ctypes
+    from oracle import make_ref
+    if not os.path.exists(make_ref.MANIFEST):
+        return None
+    man = json.load(open(make_ref.MANIFEST))
+    if tag not in man:
+        return None
+    make_ref.build()
+    ent = man[tag]
+    libs = {}
+    for role, f in ent['files'].items():
+        so = os.path.join(make_ref.REF_DIR, f['file'][:-2] + '.so')
+        if not os.path.exists(so):
+            return None
+        fn = getattr(ctypes.CDLL(so), f['kernel'])
+        fn.restype = ctypes.c_int
+        libs[role] = fn
+    return ent, libs
+
+
+def cpu_reference(steps_total, threads, tag='d3q19_e6_mrt1_64', box=None):
+    """Reference CTypes kernels, `threads` independent boxes, `steps_total` steps
+    each; returns (MLUPS aggregated, seconds, cells per box, kind)."""
+    import ctypes
+    from sclbm.profiles import droplet
+    got = _ref_kernels(tag)
+    if got is None:
+        return None
+    ent, k = got
+    box = tuple(ent['box'])
+    V = int(np.prod(box))
+    D = len(box)
+    st = []
+    for t in range(threads):
+        n = np.ascontiguousarray(droplet(box, box[0] * 10 / 64, RHO_L, RHO_G, WIDTH, SEED + t).ravel())
+        u = np.zeros(V * D)
+        pop = np.zeros(V * Q)
+        k['init'](ctypes.c_void_p(pop.ctypes.data), ctypes.c_void_p(n.ctypes.data), ctypes.c_void_p(u.ctypes.data))
+        st.append([n, np.zeros(V), pop, np.zeros(V * Q)])
+
+    def worker(s, nsteps):
+        for _ in range(nsteps):
+            n, psi, pop, pop2 = s
+            k['density'](ctypes.c_void_p(n.ctypes.data), ctypes.c_void_p(psi.ctypes.data),
+                         ctypes.c_void_p(pop.ctypes.data))
+            k['step'](ctypes.c_void_p(pop2.ctypes.data), ctypes.c_void_p(pop.ctypes.data),
+                      ctypes.c_void_p(n.ctypes.data), ctypes.c_void_p(psi.ctypes.data))
+            s[2], s[3] = pop2, pop
+
+    ths = [threading.Thread(target=worker, args=(s, steps_total)) for s in st]
+    t0 = time.perf_counter()
+    for th in ths:
+        th.start()
+    for th in ths:
+        th.join()
+    dt = time.perf_counter() - t0
+    return threads * V * steps_total / dt / 1e6, dt, V, 'reference'
+
+
+def cpu_port(steps_total, threads, box=(32, 32, 32)):
+    """The oracle port (one box per thread) when the reference kernels are absent."""
+    from oracle import oracle as O
+    from sclbm import XIStencils, FStencils
+    from sclbm.profiles import droplet
+    x, f = XIStencils['D3Q19'], FStencils['D3E6']
+    sims = []
+    for t in range(threads):
+        s = O.OracleSim(box, x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], G, rates=[1.0] * Q)
+        s.set_fields(droplet(box, box[0] * 10 / 64, RHO_L, RHO_G, WIDTH, SEED + t))
+        s.init_populations()
+        sims.append(s)
+    ths = [threading.Thread(target=s.run, args=(steps_total,)) for s in sims]
+    t0 = time.perf_counter()
+    for th in ths:
+        th.start()
+    for th in ths:
+        th.join()
+    dt = time.perf_counter() - t0
+    V = int(np.prod(box))
+    return threads * V * steps_total / dt / 1e6, dt, V, 'port'
+
+
+def cpu_measure(target_s=15.0, threads=None):
+    """Bounded CPU sample: calibrate one step, then run for about target_s."""
+    threads = threads or os.cpu_count() or 1
+    res = cpu_reference(1, threads)
+    runner = cpu_reference
+    if res is None:
+        runner = cpu_port
+        res = cpu_port(1, threads)
+    mlups, dt, V, kind = res
+    steps = max(1, int(target_s / max(dt, 1e-3)))
+    mlups, dt, V, kind = runner(steps, threads)
+    sample = '%d threads x %d steps of an independent %d-cell box (%s), %.1f s' % (
+        threads, steps, V, 'the reference\'s generated CTypes kernels' if kind == 'reference' else 'oracle port',
+        dt)
+    return {'value': round(mlups, 3), 'unit': 'MLUPS', 'cores': threads, 'kind': kind, 'sample': sample}
+
+
+# ----------------------------------------------------------------------------
+# GPU arm
+# ----------------------------------------------------------------------------
+def peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json')))
+    except Exception:
+        return None
+
+
+def make_sim(precision, device):
+    from sclbm import _lib, XIStencils, FStencils
+    x, f = XIStencils['D3Q19'], FStencils['D3E6']
+    S = np.eye(Q)
+    return _lib.Sim(3, BOX, x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], G, collision=_lib.COLL_MRT, mrt_s=S,
+                    precision=_lib.FP32_SHIFTED if precision == 'fp32' else _lib.FP64,
+                    rho0=0.5 * (RHO_L + RHO_G), device=device)
+
+
+def e2e_measure(precision, device, iters=3, lbm_steps=200):
+    """Through the public API with host buffers: H2D of the initial density and
+    velocity, InitPopulations, MainLoop over lbm_steps, GetDensityField (D2H)."""
+    from sclbm import ShanChenMultiPhase, XIStencils, FStencils, CUDA_T
+    from sclbm.profiles import droplet
+    import sympy as sp
+    ShanChenMultiPhase.verbose = False
+    n0 = droplet(BOX, R, RHO_L, RHO_G, WIDTH, SEED)
+    u0 = np.zeros(3 * n0.size)
+    sc = ShanChenMultiPhase(lang=CUDA_T, dim_sizes=BOX, xi_stencil=XIStencils['D3Q19'],
+                            f_stencil=FStencils['D3E6'], psi_code='exp(-1./ln_0)', psi_sym=None, SC_G=G,
+                            tau=1.0, precision='fp32_shifted' if precision == 'fp32' else 'fp64',
+                            rho0=0.5 * (RHO_L + RHO_G), device=device)
+    syms = [sp.Symbol('w%d' % i) for i in range(Q)]
+    mrt = dict(relaxation_matrix=sp.Matrix.diag(syms), omega_syms_vals=[(s, 1.0) for s in syms])
+    s = 4 if precision == 'fp32' else 8
+
+    def job():
+        sc.sims_idpy_memory['n'].H2D(n0)
+        sc.sims_idpy_memory['u'].H2D(u0)
+        sc.init_status['n'] = sc.init_status['u'] = True
+        sc.InitPopulations()
+        sc.MainLoopMRT([0, lbm_steps], **mrt)
+        return sc.GetDensityField()
+
+    job()  # warm-up (graph capture, staging)
+    t0 = time.perf_counter()
+    for _ in range(iters):
+        n = job()
+    dt = (time.perf_counter() - t0) / iters
+    V = n0.size
+    sc.End()
+    return {'value': round(V * lbm_steps / dt / 1e6, 1), 'unit': 'MLUPS',
+            'h2d_bytes_per_step': int(V * s * 4), 'd2h_bytes_per_step': int(V * s),
+            'step': 'one job: H2D rho and u (pinned staging), InitPopulations, MainLoopMRT over %d lattice '
+                    'steps, GetDensityField D2H' % lbm_steps,
+            'seconds_per_job': round(dt, 4), 'finite_density': bool(np.isfinite(n).all())}
+
+
+def run_ours(a, dist):
+    from sclbm.profiles import droplet
+    dev = dist.local
+    n0 = droplet(BOX, R, RHO_L, RHO_G, WIDTH, SEED + dist.rank)
+    V = n0.size
+    sim = make_sim('fp32', dev)
+    sim.set_density(n0)
+    sim.set_velocity(np.zeros(3 * V))
+    sim.init_populations()
+    sim.step(a.warmup)
+    kps = sim.kernels_per_step()
+    clocks = Clocks(dev)
+    dist.barrier()
+    sim.sync()
+    clocks.start()
+    ms = sim.step_timed(a.steps)
+    ck = clocks.stop()
+    dist.barrier()
+    ms = dist.max(ms)
+    finite, nmax = sim.density_finite()
+    # per-kernel device time of the dominant kernel (events on the handle's stream)
+    k_ms = sim.profile_step(20)
+    sim.close()
+    total = dist.ws * V * a.steps
+    mlups = total / (ms / 1e3) / 1e6
+    pk = peaks()
+    hbm = pk['hbm_gbs'] if pk else 6800.0
+    alg_bytes = 2 * Q * 4 * V                      # one read + one write of every population (FP32)
+    ach = alg_bytes / (k_ms[1] / 1e3) / 1e9
+    step_gbs = alg_bytes * a.steps / (ms / 1e3) / 1e9 / dist.ws * dist.ws
+    out = {
+        'metric': METRIC, 'value': round(mlups, 1), 'unit': 'MLUPS', 'n_gpus': dist.ws, 'steps': a.steps,
+        'warmup': a.warmup, 'ms_per_step': round(ms / a.steps, 5), 'higher_is_better': True,
+        'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+        'config': {'workload': WORKLOAD, 'box': list(BOX), 'lattice': 'D3Q19', 'stencil': 'D3E6',
+                   'collision': 'MRT (rates 1.0)', 'precision': 'FP32 deviations from w_q*rho0, FP64 reductions',
+                   'l2': 'inputs larger than L2 (populations 2 x %.2f GB)' % (Q * 4 * V / 1e9),
+                   'parallelism': 'replicas x%d' % dist.ws if dist.ws > 1 else 'single GPU'},
+        'roofline': {'bound': 'hbm', 'kernel': 'k_fcs (force+collide+push-stream pass)',
+                     'achieved': round(ach, 1), 'peak': hbm, 'unit': 'GB/s', 'frac': round(ach / hbm, 4),
+                     'peak_source': 'MEASURED_PEAKS.json hbm_gbs (measured copy)' if pk else 'fallback 6.8 TB/s',
+                     'traffic': None, 'alg_bytes_per_launch': alg_bytes,
+                     'kernel_ms': round(k_ms[1], 4), 'density_pass_ms': round(k_ms[0], 4),
+                     'step_alg_GBs': round(alg_bytes * a.steps / (ms / 1e3) / 1e9, 1),
+                     'step_frac': round(alg_bytes * a.steps / (ms / 1e3) / 1e9 / hbm, 4)},
+        'gpu_launches': int(kps * a.steps),
+        'clocks': ck,
+        'finite_density_at_end': finite, 'max_density_at_end': nmax,
+    }
+    if dist.rank == 0 and dist.ws == 1:
+        # plain FP64 path on the same workload (secondary)
+        s64 = make_sim('fp64', dev)
+        s64.set_density(n0)
+        s64.set_velocity(np.zeros(3 * V))
+        s64.init_populations()
+        s64.step(2)
+        k64 = max(4, a.steps // 50)
+        ms64 = s64.step_timed(k64)
+        kk = s64.profile_step(3)
+        s64.close()
+        out['fp64'] = {'value': round(V * k64 / (ms64 / 1e3) / 1e6, 1), 'unit': 'MLUPS', 'steps': k64,
+                       'ms_per_step': round(ms64 / k64, 4), 'kernel_ms': [round(kk[0], 4), round(kk[1], 4)],
+                       'alg_GBs': round(2 * Q * 8 * V * k64 / (ms64 / 1e3) / 1e9, 1)}
+        out['e2e'] = e2e_measure('fp32', dev)
+        if not a.no_cpu:
+            out['cpu_baseline'] = cpu_measure(a.cpu_seconds)
+    return out
+
+
+def run_reference(a, dist):
+    if dist.rank != 0:
+        return None
+    threads = os.cpu_count() or 1
+    got = _ref_kernels('d3q19_e6_mrt1_64')
+    runner = cpu_reference if got is not None else cpu_port
+    # bounded: calibrate one step, then size the per-step work to the K+W budget
+    mlups1, dt1, V, kind = runner(1, threads)
+    res = runner(a.warmup, threads) if a.warmup else None
+    mlups, dt, V, kind = runner(a.steps, threads)
+    out = {'metric': METRIC, 'value': round(mlups, 3), 'unit': 'MLUPS', 'n_gpus': dist.ws, 'steps': a.steps,
+           'warmup': a.warmup, 'ms_per_step': round(dt / a.steps * 1e3, 3), 'higher_is_better': True,
+           'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64', 'data': 'synthetic', 'impl': 'reference',
+           'config': {'workload': WORKLOAD + ' (CPU: %d-cell sample box per thread)' % V, 'threads': threads},
+           'cpu_baseline': {'value': round(mlups, 3), 'unit': 'MLUPS', 'cores': threads, 'kind': kind,
+                            'sample': '%d threads x %d steps, one independent %d-cell box each' % (
+                                threads, a.steps, V)},
+           'e2e': {'value': round(mlups, 3), 'unit': 'MLUPS', 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    return out
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=1000)
+    ap.add_argument('--warmup', type=int, default=5)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--cpu-seconds', type=float, default=15.0)
+    ap.add_argument('--no-cpu', action='store_true')
+    a = ap.parse_args()
+    if a.impl == 'reference':
+        ws, rank, _ = dist_env()
+        if rank != 0:
+            return 0
+        a.steps = max(1, a.steps)
+        # per-step sample sized so the whole run stays within a few minutes
+        a.steps, a.warmup = a.steps, a.warmup
+        out = run_reference(a, type('D', (), {'rank': 0, 'ws': ws})())
+        print(json.dumps(out))
+        return 0
+    dist = Dist()
+    out = run_ours(a, dist)
+    if dist.rank == 0:
+        print(json.dumps(out))
+    dist.close()
+    return 0
+
+
+if __name__ == '__main__':
+    sys.exit(main())

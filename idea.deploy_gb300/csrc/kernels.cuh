@@ -1,0 +1,264 @@
+// sm_103a kernels of the Shan-Chen step: SoA populations pop[q*V + g],
+// g = x + Lx*(y + Ly*z), periodic box, push streaming (as the reference,
+// idpy/LBM/Collisions.py:383-561), two passes per step:
+//   pass 1  k_density_psi : n = rho0 + sum_q g_q, psi = psi(n)
+//   pass 2  k_fcs         : Shan-Chen force, Guo-shifted velocity, collision
+//                           (expanded-operator tables), push stream
+// Real = double: plain FP64 (rho0 = 0, storage f_q).  Real = float: FP32
+// storage of the deviations g_q = f_q - w_q rho0 (the shift only enters the
+// density monomial, see coeffs.cpp).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "lattice.cuh"
+
+namespace sclbm {
+
+enum { PSI_EXP_INV = 0, PSI_ONE_MINUS_EXP = 1, PSI_IDENTITY = 2 };
+
+template <class Real>
+struct Geometry {
+    int L[3];
+    int64_t V;
+};
+
+template <class L, class S, class Real>
+struct StepParams {
+    static constexpr int D = L::D, Q = L::Q, QE = S::QE, K = Mono<L::D>::K;
+    Geometry<Real> geo;
+    Real rho0;      // storage shift (0 for FP64)
+    Real neg_g;     // -G
+    int psi_kind;
+    int a_nonzero;  // BGK: 1 - omega != 0
+    Real sw[QE][D]; // signed force weights e_{a,d} * w_a
+    Real A[Q][Q];   // population operator (BGK: diagonal used)
+    Real B[Q][K];   // monomial coefficients
+};
+
+template <class L, class Real>
+struct EqParams {
+    static constexpr int D = L::D, Q = L::Q, K = Mono<L::D>::K;
+    Geometry<Real> geo;
+    Real rho0;
+    Real B[Q][K];
+};
+
+template <class Real>
+__device__ __forceinline__ Real psi_of(int kind, Real n);
+template <>
+__device__ __forceinline__ double psi_of<double>(int kind, double n) {
+    if (kind == PSI_EXP_INV) return exp(-1. / n);
+    if (kind == PSI_ONE_MINUS_EXP) return 1. - exp(-n);
+    return n;
+}
+template <>
+__device__ __forceinline__ float psi_of<float>(int kind, float n) {
+    if (kind == PSI_EXP_INV) return expf(-1.f / n);
+    if (kind == PSI_ONE_MINUS_EXP) return 1.f - expf(-n);
+    return n;
+}
+
+__device__ __forceinline__ int wrapc(int x, int L) {
+    x += (x < 0) ? L : 0;
+    x -= (x >= L) ? L : 0;
+    return x;
+}
+
+template <int D>
+struct Cell {
+    int x, y, z;
+};
+
+template <int D>
+__device__ __forceinline__ bool cell_of(int64_t g, const int *Ls, Cell<D> &c) {
+    if (D == 2) {
+        c.x = (int)(g % Ls[0]);
+        c.y = (int)(g / Ls[0]);
+        c.z = 0;
+    } else {
+        const int64_t xy = (int64_t)Ls[0] * Ls[1];
+        c.z = (int)(g / xy);
+        const int r = (int)(g - (int64_t)c.z * xy);
+        c.y = r / Ls[0];
+        c.x = r - c.y * Ls[0];
+    }
+    return true;
+}
+
+template <int D>
+__device__ __forceinline__ int64_t index_at(const Cell<D> &c, int dx, int dy, int dz, const int *Ls) {
+    const int x = wrapc(c.x + dx, Ls[0]);
+    const int y = wrapc(c.y + dy, Ls[1]);
+    if (D == 2) return (int64_t)x + (int64_t)Ls[0] * y;
+    const int z = wrapc(c.z + dz, Ls[2]);
+    return (int64_t)x + (int64_t)Ls[0] * (y + (int64_t)Ls[1] * z);
+}
+
+// ---------------------------------------------------------------------------
+// pass 1: density (deviation) and pseudopotential
+// ---------------------------------------------------------------------------
+template <class L, class Real>
+__global__ void __launch_bounds__(256) k_density_psi(const Real *__restrict__ pop, Real *__restrict__ dn,
+                                                    Real *__restrict__ psi, Geometry<Real> geo, Real rho0,
+                                                    int psi_kind) {
+    const int64_t V = geo.V;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < V; g += (int64_t)gridDim.x * blockDim.x) {
+        Real s = pop[g];
+#pragma unroll
+        for (int q = 1; q < L::Q; q++) s += pop[(int64_t)q * V + g];
+        dn[g] = s;
+        psi[g] = psi_of<Real>(psi_kind, rho0 + s);
+    }
+}
+
+// Shan-Chen force at a cell from the psi field
+template <class L, class S, class Real, class P>
+__device__ __forceinline__ void sc_force(const Real *__restrict__ psi, const Cell<L::D> &c, int64_t g,
+                                         const P &p, Real *F) {
+    constexpr int D = L::D;
+#pragma unroll
+    for (int d = 0; d < D; d++) F[d] = Real(0);
+#pragma unroll
+    for (int a = 0; a < S::QE; a++) {
+        const int64_t nb = index_at<D>(c, S::e(a, 0), S::e(a, 1), D == 3 ? S::e(a, 2) : 0, p.geo.L);
+        const Real ps = __ldg(psi + nb);
+#pragma unroll
+        for (int d = 0; d < D; d++)
+            if (S::e(a, d) != 0) F[d] = fma(p.sw[a][d], ps, F[d]);
+    }
+    const Real s = p.neg_g * __ldg(psi + g);
+#pragma unroll
+    for (int d = 0; d < D; d++) F[d] *= s;
+}
+
+// Guo-shifted velocity: u = (sum_q xi_q f_q + F/2) / n
+template <class L, class Real>
+__device__ __forceinline__ void velocity(const Real *f, Real n, const Real *F, Real *u) {
+    constexpr int D = L::D;
+    const Real inv = Real(1) / n;
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+        Real j = Real(0);
+#pragma unroll
+        for (int q = 0; q < L::Q; q++) {
+            if (L::xi(q, d) > 0) j += f[q];
+            if (L::xi(q, d) < 0) j -= f[q];
+        }
+        u[d] = (j + Real(0.5) * F[d]) * inv;
+    }
+}
+
+template <int D, class Real>
+__device__ __forceinline__ void monomials(Real dn, Real n, const Real *u, const Real *F, Real *m) {
+    using M = Mono<D>;
+    m[0] = dn;
+#pragma unroll
+    for (int a = 0; a < D; a++) m[M::NU + a] = n * u[a];
+#pragma unroll
+    for (int a = 0; a < D; a++)
+#pragma unroll
+        for (int b = a; b < D; b++) m[M::nuu(a, b)] = m[M::NU + a] * u[b];
+#pragma unroll
+    for (int a = 0; a < D; a++) m[M::F + a] = F[a];
+#pragma unroll
+    for (int a = 0; a < D; a++)
+#pragma unroll
+        for (int b = 0; b < D; b++) m[M::FU + a * D + b] = F[a] * u[b];
+}
+
+// ---------------------------------------------------------------------------
+// pass 2: force + collision + push stream
+// ---------------------------------------------------------------------------
+template <class L, class S, bool MRT, class Real>
+__global__ void __launch_bounds__(128) k_fcs(const Real *__restrict__ pop, Real *__restrict__ pop_out,
+                                            const Real *__restrict__ dn, const Real *__restrict__ psi,
+                                            const __grid_constant__ StepParams<L, S, Real> p) {
+    constexpr int D = L::D, Q = L::Q, K = Mono<D>::K;
+    const int64_t V = p.geo.V;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < V; g += (int64_t)gridDim.x * blockDim.x) {
+        Cell<D> c;
+        cell_of<D>(g, p.geo.L, c);
+        Real F[D];
+        sc_force<L, S, Real>(psi, c, g, p, F);
+        Real f[Q];
+#pragma unroll
+        for (int q = 0; q < Q; q++) f[q] = __ldg(pop + (int64_t)q * V + g);
+        const Real d = __ldg(dn + g);
+        const Real n = p.rho0 + d;
+        Real u[D];
+        velocity<L, Real>(f, n, F, u);
+        Real m[K];
+        monomials<D, Real>(d, n, u, F, m);
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            Real acc = Real(0);
+            if (MRT) {
+#pragma unroll
+                for (int j = 0; j < Q; j++) acc = fma(p.A[q][j], f[j], acc);
+            } else if (p.a_nonzero) {
+                acc = p.A[q][q] * f[q];
+            }
+#pragma unroll
+            for (int k = 0; k < K; k++)
+                if (MRT || bgk_nonzero<L>(q, k)) acc = fma(p.B[q][k], m[k], acc);
+            const int64_t dst = index_at<D>(c, L::xi(q, 0), L::xi(q, 1), D == 3 ? L::xi(q, 2) : 0, p.geo.L);
+            pop_out[(int64_t)q * V + dst] = acc;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// moments read-back: Guo-shifted velocity (and n) after the force
+// ---------------------------------------------------------------------------
+template <class L, class S, bool MRT, class Real>
+__global__ void __launch_bounds__(128) k_velocity(const Real *__restrict__ pop, const Real *__restrict__ dn,
+                                                 const Real *__restrict__ psi, Real *__restrict__ u_out,
+                                                 const __grid_constant__ StepParams<L, S, Real> p) {
+    constexpr int D = L::D, Q = L::Q;
+    const int64_t V = p.geo.V;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < V; g += (int64_t)gridDim.x * blockDim.x) {
+        Cell<D> c;
+        cell_of<D>(g, p.geo.L, c);
+        Real F[D];
+        sc_force<L, S, Real>(psi, c, g, p, F);
+        Real f[Q];
+#pragma unroll
+        for (int q = 0; q < Q; q++) f[q] = pop[(int64_t)q * V + g];
+        const Real n = p.rho0 + dn[g];
+        Real u[D];
+        velocity<L, Real>(f, n, F, u);
+#pragma unroll
+        for (int d = 0; d < D; d++) u_out[(int64_t)d * V + g] = u[d];
+    }
+}
+
+// ---------------------------------------------------------------------------
+// equilibrium initialisation from (dn, u)
+// ---------------------------------------------------------------------------
+template <class L, class Real>
+__global__ void __launch_bounds__(128) k_init_pop(Real *__restrict__ pop, const Real *__restrict__ dn,
+                                                 const Real *__restrict__ u_in,
+                                                 const __grid_constant__ EqParams<L, Real> p) {
+    constexpr int D = L::D, Q = L::Q, K = Mono<D>::K;
+    const int64_t V = p.geo.V;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < V; g += (int64_t)gridDim.x * blockDim.x) {
+        const Real d = dn[g];
+        const Real n = p.rho0 + d;
+        Real u[D], F[D];
+#pragma unroll
+        for (int a = 0; a < D; a++) { u[a] = u_in[(int64_t)a * V + g]; F[a] = Real(0); }
+        Real m[K];
+        monomials<D, Real>(d, n, u, F, m);
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            Real acc = Real(0);
+#pragma unroll
+            for (int k = 0; k < Mono<D>::F; k++) acc = fma(p.B[q][k], m[k], acc);
+            pop[(int64_t)q * V + g] = acc;
+        }
+    }
+}
+
+}  // namespace sclbm

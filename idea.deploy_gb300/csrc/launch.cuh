@@ -1,0 +1,124 @@
+// Type-erased launchers: one KernelOps table per (lattice, stencil, collision,
+// precision).  Each lattice's instantiations live in their own translation unit
+// (k_d2q9.cu, k_d3q19_e*.cu) so they compile in parallel.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cstring>
+#include <cuda_runtime.h>
+
+#include "kernels.cuh"
+
+namespace sclbm {
+
+// host-side description the launch parameters are filled from
+struct HostSetup {
+    int L[3];
+    int64_t V;
+    double rho0;
+    double G;
+    int psi_kind;
+    const double *we;   // qe weights
+    const double *A;    // q*q
+    const double *B;    // q*K
+    const double *Beq;  // q*K
+    bool a_nonzero;
+};
+
+struct KernelOps {
+    size_t step_size, eq_size;
+    int kernels_per_step;
+    void (*fill_step)(void *params, const HostSetup &h);
+    void (*fill_eq)(void *params, const HostSetup &h);
+    cudaError_t (*density)(const void *pop, void *dn, void *psi, const void *step_params, int grid,
+                           cudaStream_t st);
+    cudaError_t (*fcs)(const void *pop, void *pop_out, const void *dn, const void *psi,
+                       const void *step_params, int grid, cudaStream_t st);
+    cudaError_t (*velocity)(const void *pop, const void *dn, const void *psi, void *u,
+                            const void *step_params, int grid, cudaStream_t st);
+    cudaError_t (*init_pop)(void *pop, const void *dn, const void *u, const void *eq_params, int grid,
+                            cudaStream_t st);
+    // occupancy-derived grid sizes (blocks) for a device with `sms` SMs
+    void (*grids)(int sms, int *density_grid, int *fcs_grid);
+};
+
+template <class L, class S, bool MRT, class Real>
+struct Ops {
+    using SP = StepParams<L, S, Real>;
+    using EP = EqParams<L, Real>;
+    static constexpr int D = L::D, Q = L::Q, K = Mono<L::D>::K;
+
+    static void fill_geo(Geometry<Real> &g, const HostSetup &h) {
+        for (int d = 0; d < 3; d++) g.L[d] = h.L[d];
+        g.V = h.V;
+    }
+    static void fill_step(void *params, const HostSetup &h) {
+        SP *p = static_cast<SP *>(params);
+        std::memset(p, 0, sizeof(SP));
+        fill_geo(p->geo, h);
+        p->rho0 = (Real)h.rho0;
+        p->neg_g = (Real)(-h.G);
+        p->psi_kind = h.psi_kind;
+        p->a_nonzero = h.a_nonzero ? 1 : 0;
+        for (int a = 0; a < S::QE; a++)
+            for (int d = 0; d < D; d++)
+                p->sw[a][d] = (Real)((double)S::e(a, d) * h.we[a]);
+        for (int i = 0; i < Q; i++)
+            for (int j = 0; j < Q; j++) p->A[i][j] = (Real)h.A[i * Q + j];
+        for (int i = 0; i < Q; i++)
+            for (int k = 0; k < K; k++) p->B[i][k] = (Real)h.B[i * K + k];
+    }
+    static void fill_eq(void *params, const HostSetup &h) {
+        EP *p = static_cast<EP *>(params);
+        std::memset(p, 0, sizeof(EP));
+        fill_geo(p->geo, h);
+        p->rho0 = (Real)h.rho0;
+        for (int i = 0; i < Q; i++)
+            for (int k = 0; k < K; k++) p->B[i][k] = (Real)h.Beq[i * K + k];
+    }
+    static cudaError_t density(const void *pop, void *dn, void *psi, const void *sp, int grid, cudaStream_t st) {
+        const SP *p = static_cast<const SP *>(sp);
+        k_density_psi<L, Real><<<grid, 256, 0, st>>>((const Real *)pop, (Real *)dn, (Real *)psi, p->geo, p->rho0,
+                                                     p->psi_kind);
+        return cudaGetLastError();
+    }
+    static cudaError_t fcs(const void *pop, void *pop_out, const void *dn, const void *psi, const void *sp, int grid,
+                           cudaStream_t st) {
+        k_fcs<L, S, MRT, Real><<<grid, 128, 0, st>>>((const Real *)pop, (Real *)pop_out, (const Real *)dn,
+                                                     (const Real *)psi, *static_cast<const SP *>(sp));
+        return cudaGetLastError();
+    }
+    static cudaError_t velocity(const void *pop, const void *dn, const void *psi, void *u, const void *sp, int grid,
+                                cudaStream_t st) {
+        k_velocity<L, S, MRT, Real><<<grid, 128, 0, st>>>((const Real *)pop, (const Real *)dn, (const Real *)psi,
+                                                          (Real *)u, *static_cast<const SP *>(sp));
+        return cudaGetLastError();
+    }
+    static cudaError_t init_pop(void *pop, const void *dn, const void *u, const void *ep, int grid, cudaStream_t st) {
+        k_init_pop<L, Real><<<grid, 128, 0, st>>>((Real *)pop, (const Real *)dn, (const Real *)u,
+                                                  *static_cast<const EP *>(ep));
+        return cudaGetLastError();
+    }
+    static void grids(int sms, int *dg, int *fg) {
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_density_psi<L, Real>, 256, 0);
+        *dg = sms * (b > 0 ? b : 1);
+        b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fcs<L, S, MRT, Real>, 128, 0);
+        *fg = sms * (b > 0 ? b : 1);
+    }
+    static const KernelOps *ops() {
+        static const KernelOps o = {sizeof(SP), sizeof(EP), 2, &fill_step, &fill_eq, &density,
+                                    &fcs, &velocity, &init_pop, &grids};
+        return &o;
+    }
+};
+
+// per translation unit: ops for (stencil order, collision, precision), or null
+const KernelOps *ops_d2q9(int order, bool mrt, bool fp32);
+const KernelOps *ops_d3q19_e4(bool mrt, bool fp32);
+const KernelOps *ops_d3q19_e6(bool mrt, bool fp32);
+const KernelOps *ops_d3q19_e8(bool mrt, bool fp32);
+
+}  // namespace sclbm

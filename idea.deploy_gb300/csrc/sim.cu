@@ -1,0 +1,920 @@
+// C ABI of the Shan-Chen step (include/sclbm.h): handle lifetime, device memory,
+// the step loop (CUDA-graph replay of the two-pass step), read-back and the FP64
+// reductions.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/sclbm.h"
+#include "coeffs.h"
+#include "launch.cuh"
+
+using namespace sclbm;
+
+namespace {
+
+thread_local std::string g_err;
+
+int fail(int code, const char *fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    std::vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    g_err = buf;
+    return code;
+}
+
+#define CUDA_TRY(call)                                                                                \
+    do {                                                                                              \
+        cudaError_t e_ = (call);                                                                      \
+        if (e_ != cudaSuccess) return fail(SCLBM_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+constexpr int RED_THREADS = 256;
+constexpr int GRAPH_STEPS = 32;  // steps per captured graph (even: buffers come back)
+
+// ---- reductions (FP64 accumulation, per-block partials, host finishes) -----
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_down_sync(0xffffffffu, v, o));
+    return v;
+}
+
+// reduce NV values per thread into out[blockIdx.x*NV + i]; op: 0 sum, 1 max
+template <int NV>
+__device__ __forceinline__ void block_reduce(double (&v)[NV], const int (&op)[NV], double *out) {
+    __shared__ double sh[NV][RED_THREADS / 32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int i = 0; i < NV; i++) {
+        v[i] = op[i] ? warp_max(v[i]) : warp_sum(v[i]);
+        if (lane == 0) sh[i][wid] = v[i];
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int i = 0; i < NV; i++) {
+            double x = lane < RED_THREADS / 32 ? sh[i][lane] : (op[i] ? -INFINITY : 0.0);
+            x = op[i] ? warp_max(x) : warp_sum(x);
+            if (lane == 0) out[blockIdx.x * NV + i] = x;
+        }
+    }
+}
+
+// mass (sum of all f) and momentum sum_q xi_q f_q
+template <class L, class Real>
+__global__ void __launch_bounds__(RED_THREADS) k_reduce_pop(const Real *__restrict__ pop, int64_t V, double rho0,
+                                                           double *out) {
+    constexpr int NV = 1 + L::D;
+    double v[NV] = {};
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < V; g += (int64_t)gridDim.x * blockDim.x) {
+        double s = 0, j[L::D] = {};
+#pragma unroll
+        for (int q = 0; q < L::Q; q++) {
+            const double f = (double)pop[(int64_t)q * V + g];
+            s += f;
+#pragma unroll
+            for (int d = 0; d < L::D; d++)
+                if (L::xi(q, d)) j[d] += L::xi(q, d) * f;
+        }
+        v[0] += s + rho0;  // sum_q w_q rho0 = rho0
+#pragma unroll
+        for (int d = 0; d < L::D; d++) v[1 + d] += j[d];
+    }
+    int op[NV] = {};
+    block_reduce<NV>(v, op, out);
+}
+
+// CheckUConvergenceSCMP: sum_d |u - u_old| summed, max |u|^2; then u_old = u
+template <class Real>
+__global__ void __launch_bounds__(RED_THREADS) k_check_u(const Real *__restrict__ u, Real *__restrict__ u_old,
+                                                        int D, int64_t V, double *out) {
+    double v[2] = {0.0, 0.0};
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < V; g += (int64_t)gridDim.x * blockDim.x) {
+        double dsum = 0, n2 = 0;
+        for (int d = 0; d < D; d++) {
+            const double a = (double)u[(int64_t)d * V + g];
+            const double b = (double)u_old[(int64_t)d * V + g];
+            n2 += a * a;
+            dsum += fabs(a - b);
+            u_old[(int64_t)d * V + g] = u[(int64_t)d * V + g];
+        }
+        v[0] += dsum;
+        v[1] = fmax(v[1], n2);
+    }
+    int op[2] = {0, 1};
+    block_reduce<2>(v, op, out);
+}
+
+// mass and first moments of the density (centre of mass)
+template <class Real>
+__global__ void __launch_bounds__(RED_THREADS) k_com(const Real *__restrict__ dn, double rho0, int D, int L0, int L1,
+                                                    int64_t V, double *out) {
+    double v[4] = {0, 0, 0, 0};
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < V; g += (int64_t)gridDim.x * blockDim.x) {
+        const double n = rho0 + (double)dn[g];
+        const int x = (int)(g % L0);
+        const int y = (int)((g / L0) % L1);
+        const int z = (int)(g / ((int64_t)L0 * L1));
+        v[0] += n;
+        v[1] += n * x;
+        v[2] += n * y;
+        v[3] += D == 3 ? n * z : 0.0;
+    }
+    int op[4] = {0, 0, 0, 0};
+    block_reduce<4>(v, op, out);
+}
+
+template <class Real>
+__global__ void __launch_bounds__(RED_THREADS) k_finite(const Real *__restrict__ dn, double rho0, int64_t V,
+                                                       double *out) {
+    double v[2] = {0.0, 0.0};
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < V; g += (int64_t)gridDim.x * blockDim.x) {
+        const double n = rho0 + (double)dn[g];
+        if (!isfinite(n)) v[0] = 1.0;
+        else v[1] = fmax(v[1], fabs(n));
+    }
+    int op[2] = {1, 1};
+    block_reduce<2>(v, op, out);
+}
+
+// ---- initial profiles (idpy/LBM/MultiPhaseKernels.py:44-112,605-777) -----
+enum { PROF_RADIAL = 0, PROF_FLAT = 1, PROF_SINGLE_FLAT = 2, PROF_CYLINDER = 3 };
+
+template <class Real>
+__global__ void k_profile(Real *__restrict__ dn, Real *__restrict__ u, int kind, int D, int L0, int L1, int L2,
+                          int64_t V, double n_g, double n_l, double R, double width, int dir, int full, double rho0) {
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < V; g += (int64_t)gridDim.x * blockDim.x) {
+        int pos[3];
+        pos[0] = (int)(g % L0);
+        pos[1] = (int)((g / L0) % L1);
+        pos[2] = D == 3 ? (int)(g / ((int64_t)L0 * L1)) : 0;
+        const int Ls[3] = {L0, L1, L2};
+        const double dnv = full ? (n_l - n_g) : (n_g - n_l);
+        double n = 0;
+        if (kind == PROF_RADIAL || kind == PROF_CYLINDER) {
+            int r2 = 0;
+            for (int d = 0; d < D; d++) {
+                if (kind == PROF_CYLINDER && d == dir) continue;
+                const int t = Ls[d] / 2 - pos[d];
+                r2 += t * t;
+            }
+            const double r = sqrt((double)r2);
+            n = 0.5 * (n_g + n_l) - 0.5 * dnv * tanh(r - R);
+        } else if (kind == PROF_FLAT) {
+            const int L = Ls[dir], x = pos[dir], x0 = L / 2, xm = L / 2;
+            int xp;
+            if (x0 - xm >= 0) xp = (x < x0 - xm) ? x - (x0 - xm) + L : x - (x0 - xm);
+            else xp = (x < x0 + xm) ? x - (x0 + xm) + L : x - (x0 + xm);
+            const double prof = tanh((double)xp - (xm - 0.5 * width)) - tanh((double)xp - (xm + 0.5 * width));
+            n = 0.5 * (n_g + n_l) + 0.5 * dnv * (prof - 1.0);
+        } else {
+            const int x0 = Ls[dir] / 2;
+            n = n_g + dnv * ((tanh((double)(pos[dir] - x0)) + 1.0) * 0.5);
+        }
+        dn[g] = (Real)(n - rho0);
+        for (int d = 0; d < D; d++) u[(int64_t)d * V + g] = Real(0);
+    }
+}
+
+}  // namespace
+
+// ============================================================================
+struct sclbm_sim {
+    int device = 0;
+    cudaStream_t st = nullptr;
+    int D = 0, Q = 0, QE = 0, K = 0, order = 0;
+    int L[3] = {1, 1, 1};
+    int64_t V = 0;
+    bool fp32 = false, mrt = false;
+    size_t rs = 8;
+    double rho0 = 0, c2 = 1.0 / 3, G = 0;
+    std::vector<double> w, we;
+    std::vector<int> xi, e;
+    int psi_kind = 0, literals = 0, sms = 1;
+    const KernelOps *ops = nullptr;
+    std::vector<unsigned char> sp, ep;  // launch parameter blocks
+    void *pop[2] = {nullptr, nullptr};
+    int cur = 0;
+    void *dn = nullptr, *psi = nullptr, *u = nullptr, *u_old = nullptr;
+    double *red = nullptr;
+    int red_blocks = 0;
+    int dgrid = 0, fgrid = 0, ugrid = 0;
+    bool n_set = false, u_set = false, pop_set = false, moments_fresh = false;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    int64_t device_bytes = 0;
+    void *stage = nullptr;  // pinned host staging buffer (lazy)
+    cudaEvent_t stage_ev[2] = {nullptr, nullptr};
+};
+
+namespace {
+
+struct DevGuard {
+    int prev = -1;
+    explicit DevGuard(int dev) {
+        cudaGetDevice(&prev);
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DevGuard() {
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+};
+
+int alloc(sclbm_sim *s, void **p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return fail(SCLBM_ERR_NOMEM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
+    }
+    s->device_bytes += (int64_t)bytes;
+    return SCLBM_OK;
+}
+
+void release(sclbm_sim *s) {
+    for (auto &g : s->graph)
+        if (g) cudaGraphExecDestroy(g), g = nullptr;
+    for (void *p : {s->pop[0], s->pop[1], s->dn, s->psi, s->u, s->u_old, (void *)s->red})
+        if (p) cudaFree(p);
+    for (auto &ev : s->stage_ev)
+        if (ev) cudaEventDestroy(ev), ev = nullptr;
+    if (s->stage) cudaFreeHost(s->stage);
+    if (s->st) cudaStreamDestroy(s->st);
+}
+
+const int *compiled_xi(int D, int q) {
+    static int t2[9 * 2], t3[19 * 3];
+    static bool init = false;
+    if (!init) {
+        for (int i = 0; i < 9; i++)
+            for (int d = 0; d < 2; d++) t2[i * 2 + d] = D2Q9::xi(i, d);
+        for (int i = 0; i < 19; i++)
+            for (int d = 0; d < 3; d++) t3[i * 3 + d] = D3Q19::xi(i, d);
+        init = true;
+    }
+    if (D == 2 && q == 9) return t2;
+    if (D == 3 && q == 19) return t3;
+    return nullptr;
+}
+
+template <class S>
+bool stencil_is(const int *e, int qe) {
+    if (qe != S::QE) return false;
+    for (int a = 0; a < qe; a++)
+        for (int d = 0; d < S::D; d++)
+            if (e[a * S::D + d] != S::e(a, d)) return false;
+    return true;
+}
+
+int stencil_order(int D, const int *e, int qe) {
+    if (D == 2) {
+        if (stencil_is<D2E4>(e, qe)) return 4;
+        if (stencil_is<D2E6>(e, qe)) return 6;
+        if (stencil_is<D2E8>(e, qe)) return 8;
+    } else {
+        if (stencil_is<D3E4>(e, qe)) return 4;
+        if (stencil_is<D3E6>(e, qe)) return 6;
+        if (stencil_is<D3E8>(e, qe)) return 8;
+    }
+    return 0;
+}
+
+int launch_step(sclbm_sim *s) {
+    const KernelOps *o = s->ops;
+    cudaError_t e = o->density(s->pop[s->cur], s->dn, s->psi, s->sp.data(), s->dgrid, s->st);
+    if (e == cudaSuccess) e = o->fcs(s->pop[s->cur], s->pop[s->cur ^ 1], s->dn, s->psi, s->sp.data(), s->fgrid, s->st);
+    if (e != cudaSuccess) return fail(SCLBM_ERR_CUDA, "step launch: %s", cudaGetErrorString(e));
+    s->cur ^= 1;
+    return SCLBM_OK;
+}
+
+int build_graph(sclbm_sim *s, int parity) {
+    const int saved = s->cur;
+    s->cur = parity;
+    cudaGraph_t g = nullptr;
+    CUDA_TRY(cudaStreamBeginCapture(s->st, cudaStreamCaptureModeThreadLocal));
+    int rc = SCLBM_OK;
+    for (int i = 0; i < GRAPH_STEPS && rc == SCLBM_OK; i++) rc = launch_step(s);
+    cudaError_t ce = cudaStreamEndCapture(s->st, &g);
+    s->cur = saved;
+    if (rc != SCLBM_OK) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+    }
+    if (ce != cudaSuccess) return fail(SCLBM_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+    ce = cudaGraphInstantiate(&s->graph[parity], g, 0);
+    cudaGraphDestroy(g);
+    if (ce != cudaSuccess) return fail(SCLBM_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+    return SCLBM_OK;
+}
+
+int run_steps(sclbm_sim *s, int64_t n) {
+    while (n >= GRAPH_STEPS) {
+        if (!s->graph[s->cur]) {
+            int rc = build_graph(s, s->cur);
+            if (rc) return rc;
+        }
+        CUDA_TRY(cudaGraphLaunch(s->graph[s->cur], s->st));
+        n -= GRAPH_STEPS;  // even number of steps: s->cur unchanged
+    }
+    for (int64_t i = 0; i < n; i++) {
+        int rc = launch_step(s);
+        if (rc) return rc;
+    }
+    return SCLBM_OK;
+}
+
+// Host <-> device transfers go through a pinned staging buffer in two halves
+// (double-buffered: the copy of one chunk overlaps the conversion of the
+// other).  Device arrays hold Real (FP64, or FP32 deviations); host arrays are
+// FP64 values, minus / plus an optional per-plane shift (w_q rho0, rho0).
+constexpr size_t STAGE_BYTES = size_t(32) << 20;
+
+int ensure_stage(sclbm_sim *s) {
+    if (s->stage) return SCLBM_OK;
+    cudaError_t e = cudaMallocHost(&s->stage, STAGE_BYTES);
+    if (e != cudaSuccess) {
+        s->stage = nullptr;
+        cudaGetLastError();
+        return fail(SCLBM_ERR_NOMEM, "pinned staging buffer: %s", cudaGetErrorString(e));
+    }
+    for (auto &ev : s->stage_ev) {
+        e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming);
+        if (e != cudaSuccess) return fail(SCLBM_ERR_CUDA, "staging event: %s", cudaGetErrorString(e));
+    }
+    return SCLBM_OK;
+}
+
+inline double shift_at(const double *plane_shift, int64_t i, int64_t plane) {
+    return plane_shift ? plane_shift[i / plane] : 0.0;
+}
+
+int d2h_real(sclbm_sim *s, const void *src, double *dst, int64_t count, const double *plane_shift, int64_t plane) {
+    int rc = ensure_stage(s);
+    if (rc) return rc;
+    const int64_t per = (int64_t)(STAGE_BYTES / 2 / s->rs);
+    const int64_t nchunk = (count + per - 1) / per;
+    char *half[2] = {(char *)s->stage, (char *)s->stage + STAGE_BYTES / 2};
+    auto issue = [&](int64_t c) -> cudaError_t {
+        const int64_t off = c * per, len = std::min(per, count - off);
+        cudaError_t e = cudaMemcpyAsync(half[c & 1], (const char *)src + off * s->rs, len * s->rs,
+                                        cudaMemcpyDeviceToHost, s->st);
+        if (e == cudaSuccess) e = cudaEventRecord(s->stage_ev[c & 1], s->st);
+        return e;
+    };
+    if (nchunk > 0) CUDA_TRY(issue(0));
+    for (int64_t c = 0; c < nchunk; c++) {
+        CUDA_TRY(cudaEventSynchronize(s->stage_ev[c & 1]));
+        if (c + 1 < nchunk) CUDA_TRY(issue(c + 1));
+        const int64_t off = c * per, len = std::min(per, count - off);
+        if (s->fp32) {
+            const float *h = (const float *)half[c & 1];
+            for (int64_t i = 0; i < len; i++) dst[off + i] = (double)h[i] + shift_at(plane_shift, off + i, plane);
+        } else {
+            const double *h = (const double *)half[c & 1];
+            for (int64_t i = 0; i < len; i++) dst[off + i] = h[i] + shift_at(plane_shift, off + i, plane);
+        }
+    }
+    return SCLBM_OK;
+}
+
+int h2d_real(sclbm_sim *s, void *dst, const double *src, int64_t count, const double *plane_shift, int64_t plane) {
+    int rc = ensure_stage(s);
+    if (rc) return rc;
+    const int64_t per = (int64_t)(STAGE_BYTES / 2 / s->rs);
+    const int64_t nchunk = (count + per - 1) / per;
+    char *half[2] = {(char *)s->stage, (char *)s->stage + STAGE_BYTES / 2};
+    for (int64_t c = 0; c < nchunk; c++) {
+        if (c >= 2) CUDA_TRY(cudaEventSynchronize(s->stage_ev[c & 1]));  // half free again
+        const int64_t off = c * per, len = std::min(per, count - off);
+        if (s->fp32) {
+            float *h = (float *)half[c & 1];
+            for (int64_t i = 0; i < len; i++) h[i] = (float)(src[off + i] - shift_at(plane_shift, off + i, plane));
+        } else {
+            double *h = (double *)half[c & 1];
+            for (int64_t i = 0; i < len; i++) h[i] = src[off + i] - shift_at(plane_shift, off + i, plane);
+        }
+        CUDA_TRY(cudaMemcpyAsync((char *)dst + off * s->rs, half[c & 1], len * s->rs, cudaMemcpyHostToDevice,
+                                 s->st));
+        CUDA_TRY(cudaEventRecord(s->stage_ev[c & 1], s->st));
+    }
+    CUDA_TRY(cudaStreamSynchronize(s->st));
+    return SCLBM_OK;
+}
+
+int finish_partials(sclbm_sim *s, int nv, std::vector<double> &part) {
+    part.resize((size_t)s->red_blocks * nv);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaMemcpyAsync(part.data(), s->red, part.size() * sizeof(double), cudaMemcpyDeviceToHost, s->st));
+    CUDA_TRY(cudaStreamSynchronize(s->st));
+    return SCLBM_OK;
+}
+
+int init_pop(sclbm_sim *s) {
+    cudaError_t e = s->ops->init_pop(s->pop[s->cur], s->dn, s->u, s->ep.data(), s->fgrid, s->st);
+    if (e != cudaSuccess) return fail(SCLBM_ERR_CUDA, "init populations: %s", cudaGetErrorString(e));
+    CUDA_TRY(cudaStreamSynchronize(s->st));
+    s->pop_set = true;
+    s->moments_fresh = false;
+    return SCLBM_OK;
+}
+
+int profile(sclbm_sim *s, int kind, double n_g, double n_l, double R, double width, int dir, int full) {
+    if (!s) return fail(SCLBM_ERR_ARG, "null handle");
+    if (dir < 0 || dir >= s->D) return fail(SCLBM_ERR_ARG, "direction %d out of range", dir);
+    DevGuard dg(s->device);
+    if (s->fp32)
+        k_profile<float><<<s->red_blocks, RED_THREADS, 0, s->st>>>((float *)s->dn, (float *)s->u, kind, s->D, s->L[0],
+                                                                   s->L[1], s->L[2], s->V, n_g, n_l, R, width, dir,
+                                                                   full, s->rho0);
+    else
+        k_profile<double><<<s->red_blocks, RED_THREADS, 0, s->st>>>((double *)s->dn, (double *)s->u, kind, s->D,
+                                                                    s->L[0], s->L[1], s->L[2], s->V, n_g, n_l, R,
+                                                                    width, dir, full, s->rho0);
+    CUDA_TRY(cudaGetLastError());
+    s->n_set = s->u_set = true;
+    return init_pop(s);
+}
+
+
+// build the collision operator and launch parameters; pick the kernel set
+int configure(sclbm_sim *s, int collision, double tau, const double *mrt_s, const double *coll_a,
+              const double *coll_b) {
+    if (collision != SCLBM_COLL_BGK && collision != SCLBM_COLL_MRT)
+        return fail(SCLBM_ERR_ARG, "collision %d", collision);
+    if ((coll_a == nullptr) != (coll_b == nullptr)) return fail(SCLBM_ERR_ARG, "coll_a and coll_b go together");
+    if (collision == SCLBM_COLL_BGK && !coll_a && !(tau > 0)) return fail(SCLBM_ERR_ARG, "tau must be > 0");
+    if (collision == SCLBM_COLL_MRT && !coll_a && !mrt_s)
+        return fail(SCLBM_ERR_ARG, "MRT needs the relaxation matrix mrt_s");
+    CollisionSpec cs;
+    cs.dim = s->D;
+    cs.q = s->Q;
+    cs.xi = s->xi.data();
+    cs.w = s->w.data();
+    cs.c2 = s->c2;
+    cs.collision = coll_a ? SCLBM_COLL_BGK : collision;  // equilibrium table always built
+    cs.tau = coll_a ? 1.0 : tau;
+    cs.mrt_s = mrt_s;
+    cs.literals = s->fp32 ? SCLBM_LIT_EXACT : s->literals;
+    CollisionTables t;
+    std::string err;
+    if (build_collision(cs, t, err)) return fail(SCLBM_ERR_UNSUPPORTED, "collision operator: %s", err.c_str());
+    if (coll_a) {
+        t.A.assign(coll_a, coll_a + (size_t)s->Q * s->Q);
+        t.B.assign(coll_b, coll_b + (size_t)s->Q * t.K);
+    }
+    const bool mrt = collision == SCLBM_COLL_MRT || coll_a != nullptr;
+    const KernelOps *ops = nullptr;
+    if (s->D == 2) ops = ops_d2q9(s->order, mrt, s->fp32);
+    else if (s->order == 4) ops = ops_d3q19_e4(mrt, s->fp32);
+    else if (s->order == 6) ops = ops_d3q19_e6(mrt, s->fp32);
+    else ops = ops_d3q19_e8(mrt, s->fp32);
+    if (!ops) return fail(SCLBM_ERR_UNSUPPORTED, "no kernels for this configuration");
+    bool a_nonzero = false;
+    for (int q = 0; q < s->Q; q++) a_nonzero = a_nonzero || t.A[(size_t)q * s->Q + q] != 0.0;
+    HostSetup h;
+    for (int d = 0; d < 3; d++) h.L[d] = d < s->D ? s->L[d] : 1;
+    h.V = s->V;
+    h.rho0 = s->rho0;
+    h.G = s->G;
+    h.psi_kind = s->psi_kind;
+    h.we = s->we.data();
+    h.A = t.A.data();
+    h.B = t.B.data();
+    h.Beq = t.Beq.data();
+    h.a_nonzero = a_nonzero;
+    for (auto &g : s->graph)
+        if (g) cudaGraphExecDestroy(g), g = nullptr;
+    s->K = t.K;
+    s->mrt = mrt;
+    s->ops = ops;
+    s->sp.assign(ops->step_size, 0);
+    s->ep.assign(ops->eq_size, 0);
+    ops->fill_step(s->sp.data(), h);
+    ops->fill_eq(s->ep.data(), h);
+    ops->grids(s->sms, &s->dgrid, &s->fgrid);
+    const int64_t need_d = (s->V + 255) / 256, need_f = (s->V + 127) / 128;
+    s->dgrid = (int)std::max<int64_t>(1, std::min<int64_t>(s->dgrid, need_d));
+    s->fgrid = (int)std::max<int64_t>(1, std::min<int64_t>(s->fgrid, need_f));
+    return SCLBM_OK;
+}
+
+}  // namespace
+
+// ============================================================================
+extern "C" {
+
+const char *sclbm_version(void) { return "sclbm 0.1 (sm_103a)"; }
+
+const char *sclbm_status_string(int st) {
+    switch (st) {
+    case SCLBM_OK: return "ok";
+    case SCLBM_ERR_ARG: return "invalid argument";
+    case SCLBM_ERR_UNSUPPORTED: return "unsupported configuration";
+    case SCLBM_ERR_CUDA: return "CUDA error";
+    case SCLBM_ERR_STATE: return "call out of order";
+    case SCLBM_ERR_NOMEM: return "out of device memory";
+    case SCLBM_ERR_NODEVICE: return "no usable device";
+    default: return "unknown status";
+    }
+}
+
+const char *sclbm_last_error(void) { return g_err.c_str(); }
+
+int sclbm_monomial_count(int dim) {
+    if (dim == 2) return Mono<2>::K;
+    if (dim == 3) return Mono<3>::K;
+    return 0;
+}
+
+int sclbm_create(const sclbm_params *p, sclbm_sim **out) {
+    g_err.clear();
+    if (!p || !out) return fail(SCLBM_ERR_ARG, "null argument");
+    *out = nullptr;
+    if (p->dim != 2 && p->dim != 3) return fail(SCLBM_ERR_UNSUPPORTED, "dimension %d (2 or 3 supported)", p->dim);
+    if (!p->xi || !p->w || !p->e || !p->we) return fail(SCLBM_ERR_ARG, "null stencil table");
+    const int *cx = compiled_xi(p->dim, p->q);
+    if (!cx) return fail(SCLBM_ERR_UNSUPPORTED, "lattice D%dQ%d not built (D2Q9, D3Q19)", p->dim, p->q);
+    for (int i = 0; i < p->q * p->dim; i++)
+        if (p->xi[i] != cx[i]) return fail(SCLBM_ERR_UNSUPPORTED, "lattice velocities differ from D%dQ%d", p->dim, p->q);
+    const int order = stencil_order(p->dim, p->e, p->qe);
+    if (!order) return fail(SCLBM_ERR_UNSUPPORTED, "force stencil (%d vectors) is not E4/E6/E8", p->qe);
+    for (int d = 0; d < p->dim; d++)
+        if (p->sizes[d] < 2 || p->sizes[d] > (1 << 24))
+            return fail(SCLBM_ERR_ARG, "size[%d] = %d out of range [2, 2^24]", d, p->sizes[d]);
+    if (p->psi_kind < 0 || p->psi_kind > 2) return fail(SCLBM_ERR_ARG, "psi_kind %d", p->psi_kind);
+    if (p->precision != SCLBM_FP64 && p->precision != SCLBM_FP32_SHIFTED)
+        return fail(SCLBM_ERR_ARG, "precision %d", p->precision);
+    if (!(p->c2 > 0)) return fail(SCLBM_ERR_ARG, "c2 must be > 0");
+
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(SCLBM_ERR_NODEVICE, "no CUDA device visible");
+    }
+    if (p->device < 0 || p->device >= ndev) return fail(SCLBM_ERR_ARG, "device %d of %d", p->device, ndev);
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, p->device) != cudaSuccess) return fail(SCLBM_ERR_CUDA, "device properties");
+    if (prop.major < 10) return fail(SCLBM_ERR_NODEVICE, "device %s is sm_%d%d; built for sm_103a", prop.name,
+                                     prop.major, prop.minor);
+
+    if (p->collision != SCLBM_COLL_BGK && p->collision != SCLBM_COLL_MRT)
+        return fail(SCLBM_ERR_ARG, "collision %d", p->collision);
+    sclbm_sim *s = new sclbm_sim();
+    s->device = p->device;
+    DevGuard dg(s->device);
+    s->D = p->dim;
+    s->Q = p->q;
+    s->QE = p->qe;
+    s->order = order;
+    s->V = 1;
+    for (int d = 0; d < s->D; d++) {
+        s->L[d] = p->sizes[d];
+        s->V *= p->sizes[d];
+    }
+    s->fp32 = p->precision == SCLBM_FP32_SHIFTED;
+    s->rs = s->fp32 ? 4 : 8;
+    s->rho0 = s->fp32 ? p->rho0 : 0.0;
+    s->c2 = p->c2;
+    s->G = p->sc_g;
+    s->psi_kind = p->psi_kind;
+    s->literals = p->literals;
+    s->sms = prop.multiProcessorCount;
+    s->w.assign(p->w, p->w + p->q);
+    s->we.assign(p->we, p->we + p->qe);
+    s->xi.assign(p->xi, p->xi + p->q * p->dim);
+    s->e.assign(p->e, p->e + p->qe * p->dim);
+    {
+        int rc0 = configure(s, p->collision, p->tau, p->mrt_s, p->coll_a, p->coll_b);
+        if (rc0) {
+            delete s;
+            return rc0;
+        }
+    }
+
+    int rc = SCLBM_OK;
+    if (cudaStreamCreateWithFlags(&s->st, cudaStreamNonBlocking) != cudaSuccess) {
+        cudaGetLastError();
+        rc = fail(SCLBM_ERR_CUDA, "stream create");
+    }
+    const size_t pb = (size_t)s->V * s->Q * s->rs, fb = (size_t)s->V * s->rs;
+    if (!rc) rc = alloc(s, &s->pop[0], pb);
+    if (!rc) rc = alloc(s, &s->pop[1], pb);
+    if (!rc) rc = alloc(s, &s->dn, fb);
+    if (!rc) rc = alloc(s, &s->psi, fb);
+    if (!rc) rc = alloc(s, &s->u, fb * s->D);
+    if (!rc) rc = alloc(s, &s->u_old, fb * s->D);
+    s->red_blocks = prop.multiProcessorCount * 2;
+    if (!rc) rc = alloc(s, (void **)&s->red, (size_t)s->red_blocks * 8 * sizeof(double));
+    if (!rc) {
+        if (cudaMemsetAsync(s->u, 0, fb * s->D, s->st) != cudaSuccess ||
+            cudaMemsetAsync(s->u_old, 0, fb * s->D, s->st) != cudaSuccess ||
+            cudaMemsetAsync(s->dn, 0, fb, s->st) != cudaSuccess ||
+            cudaStreamSynchronize(s->st) != cudaSuccess)
+            rc = fail(SCLBM_ERR_CUDA, "memset: %s", cudaGetErrorString(cudaGetLastError()));
+    }
+    if (rc) {
+        release(s);
+        delete s;
+        return rc;
+    }
+    *out = s;
+    return SCLBM_OK;
+}
+
+int sclbm_destroy(sclbm_sim *s) {
+    if (!s) return SCLBM_OK;
+    {
+        DevGuard dg(s->device);
+        cudaStreamSynchronize(s->st);
+        release(s);
+    }
+    delete s;
+    return SCLBM_OK;
+}
+
+int sclbm_info(const sclbm_sim *s, int64_t *volume, int64_t *device_bytes) {
+    if (!s) return fail(SCLBM_ERR_ARG, "null handle");
+    if (volume) *volume = s->V;
+    if (device_bytes) *device_bytes = s->device_bytes;
+    return SCLBM_OK;
+}
+
+int sclbm_kernels_per_step(const sclbm_sim *s, int *count) {
+    if (!s || !count) return fail(SCLBM_ERR_ARG, "null argument");
+    *count = s->ops->kernels_per_step;
+    return SCLBM_OK;
+}
+
+int sclbm_set_collision(sclbm_sim *s, int collision, double tau, const double *mrt_s, const double *coll_a,
+                        const double *coll_b) {
+    if (!s) return fail(SCLBM_ERR_ARG, "null handle");
+    DevGuard dg(s->device);
+    CUDA_TRY(cudaStreamSynchronize(s->st));
+    return configure(s, collision, tau, mrt_s, coll_a, coll_b);
+}
+
+int sclbm_set_density(sclbm_sim *s, const double *n) {
+    if (!s || !n) return fail(SCLBM_ERR_ARG, "null argument");
+    DevGuard dg(s->device);
+    double shift = s->rho0;
+    int rc = h2d_real(s, s->dn, n, s->V, s->fp32 ? &shift : nullptr, s->V);
+    if (!rc) s->n_set = true;
+    return rc;
+}
+
+int sclbm_set_velocity(sclbm_sim *s, const double *u) {
+    if (!s || !u) return fail(SCLBM_ERR_ARG, "null argument");
+    DevGuard dg(s->device);
+    int rc = h2d_real(s, s->u, u, s->V * s->D, nullptr, s->V);
+    if (!rc) s->u_set = true;
+    return rc;
+}
+
+int sclbm_get_density(sclbm_sim *s, double *n) {
+    if (!s || !n) return fail(SCLBM_ERR_ARG, "null argument");
+    DevGuard dg(s->device);
+    double shift = s->rho0;
+    return d2h_real(s, s->dn, n, s->V, s->fp32 ? &shift : nullptr, s->V);
+}
+
+int sclbm_get_velocity(sclbm_sim *s, double *u) {
+    if (!s || !u) return fail(SCLBM_ERR_ARG, "null argument");
+    DevGuard dg(s->device);
+    return d2h_real(s, s->u, u, s->V * s->D, nullptr, s->V);
+}
+
+int sclbm_get_populations(sclbm_sim *s, double *pop) {
+    if (!s || !pop) return fail(SCLBM_ERR_ARG, "null argument");
+    DevGuard dg(s->device);
+    std::vector<double> shift(s->Q);
+    for (int q = 0; q < s->Q; q++) shift[q] = s->w[q] * s->rho0;
+    return d2h_real(s, s->pop[s->cur], pop, s->V * s->Q, s->fp32 ? shift.data() : nullptr, s->V);
+}
+
+int sclbm_set_populations(sclbm_sim *s, const double *pop) {
+    if (!s || !pop) return fail(SCLBM_ERR_ARG, "null argument");
+    DevGuard dg(s->device);
+    std::vector<double> shift(s->Q);
+    for (int q = 0; q < s->Q; q++) shift[q] = s->w[q] * s->rho0;
+    int rc = h2d_real(s, s->pop[s->cur], pop, s->V * s->Q, s->fp32 ? shift.data() : nullptr, s->V);
+    if (!rc) {
+        s->pop_set = true;
+        s->moments_fresh = false;
+    }
+    return rc;
+}
+
+int sclbm_init_populations(sclbm_sim *s) {
+    // n and u start at zero after create, as the reference's zero-filled arrays
+    if (!s) return fail(SCLBM_ERR_ARG, "null handle");
+    DevGuard dg(s->device);
+    return init_pop(s);
+}
+
+int sclbm_init_radial(sclbm_sim *s, double n_g, double n_l, double R, int full_flag) {
+    return profile(s, PROF_RADIAL, n_g, n_l, R, 0, 0, full_flag ? 1 : 0);
+}
+int sclbm_init_flat(sclbm_sim *s, double n_g, double n_l, double width, int direction, int full_flag) {
+    return profile(s, PROF_FLAT, n_g, n_l, 0, width, direction, full_flag ? 1 : 0);
+}
+int sclbm_init_single_flat(sclbm_sim *s, double n_g, double n_l, int direction, int full_flag) {
+    return profile(s, PROF_SINGLE_FLAT, n_g, n_l, 0, 0, direction, full_flag ? 1 : 0);
+}
+int sclbm_init_cylinder(sclbm_sim *s, double n_g, double n_l, double R, int direction, int full_flag) {
+    return profile(s, PROF_CYLINDER, n_g, n_l, R, 0, direction, full_flag ? 1 : 0);
+}
+
+int sclbm_step(sclbm_sim *s, int64_t nsteps) {
+    if (!s) return fail(SCLBM_ERR_ARG, "null handle");
+    if (nsteps < 0) return fail(SCLBM_ERR_ARG, "nsteps < 0");
+    if (!s->pop_set) return fail(SCLBM_ERR_STATE, "populations are not initialized");
+    DevGuard dg(s->device);
+    s->moments_fresh = false;
+    return run_steps(s, nsteps);
+}
+
+int sclbm_sync(sclbm_sim *s) {
+    if (!s) return fail(SCLBM_ERR_ARG, "null handle");
+    DevGuard dg(s->device);
+    CUDA_TRY(cudaStreamSynchronize(s->st));
+    return SCLBM_OK;
+}
+
+int sclbm_step_timed(sclbm_sim *s, int64_t nsteps, double *ms) {
+    if (!s || !ms) return fail(SCLBM_ERR_ARG, "null argument");
+    if (!s->pop_set) return fail(SCLBM_ERR_STATE, "populations are not initialized");
+    DevGuard dg(s->device);
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    CUDA_TRY(cudaEventRecord(e0, s->st));
+    int rc = run_steps(s, nsteps);
+    cudaEventRecord(e1, s->st);
+    cudaEventSynchronize(e1);
+    float t = 0;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    s->moments_fresh = false;
+    *ms = t;
+    if (rc) return rc;
+    CUDA_TRY(cudaGetLastError());
+    return SCLBM_OK;
+}
+
+int sclbm_profile_step(sclbm_sim *s, int64_t nsteps, double *ms, int nms) {
+    if (!s || !ms || nms < 2) return fail(SCLBM_ERR_ARG, "bad argument");
+    if (!s->pop_set) return fail(SCLBM_ERR_STATE, "populations are not initialized");
+    if (nsteps < 1 || nsteps > 4096) return fail(SCLBM_ERR_ARG, "nsteps in [1, 4096]");
+    DevGuard dg(s->device);
+    std::vector<cudaEvent_t> ev((size_t)nsteps * 3);
+    for (auto &e : ev) CUDA_TRY(cudaEventCreate(&e));
+    const KernelOps *o = s->ops;
+    for (int64_t i = 0; i < nsteps; i++) {
+        cudaEventRecord(ev[3 * i], s->st);
+        o->density(s->pop[s->cur], s->dn, s->psi, s->sp.data(), s->dgrid, s->st);
+        cudaEventRecord(ev[3 * i + 1], s->st);
+        o->fcs(s->pop[s->cur], s->pop[s->cur ^ 1], s->dn, s->psi, s->sp.data(), s->fgrid, s->st);
+        cudaEventRecord(ev[3 * i + 2], s->st);
+        s->cur ^= 1;
+    }
+    cudaError_t ce = cudaStreamSynchronize(s->st);
+    double t0 = 0, t1 = 0;
+    for (int64_t i = 0; i < nsteps && ce == cudaSuccess; i++) {
+        float a = 0, b = 0;
+        cudaEventElapsedTime(&a, ev[3 * i], ev[3 * i + 1]);
+        cudaEventElapsedTime(&b, ev[3 * i + 1], ev[3 * i + 2]);
+        t0 += a;
+        t1 += b;
+    }
+    for (auto &e : ev) cudaEventDestroy(e);
+    s->moments_fresh = false;
+    if (ce != cudaSuccess) return fail(SCLBM_ERR_CUDA, "profile: %s", cudaGetErrorString(ce));
+    ms[0] = t0 / nsteps;
+    ms[1] = t1 / nsteps;
+    return SCLBM_OK;
+}
+
+int sclbm_compute_moments(sclbm_sim *s) {
+    if (!s) return fail(SCLBM_ERR_ARG, "null handle");
+    if (!s->pop_set) return fail(SCLBM_ERR_STATE, "populations are not initialized");
+    DevGuard dg(s->device);
+    cudaError_t e = s->ops->density(s->pop[s->cur], s->dn, s->psi, s->sp.data(), s->dgrid, s->st);
+    if (e == cudaSuccess) e = s->ops->velocity(s->pop[s->cur], s->dn, s->psi, s->u, s->sp.data(), s->fgrid, s->st);
+    if (e != cudaSuccess) return fail(SCLBM_ERR_CUDA, "moments: %s", cudaGetErrorString(e));
+    CUDA_TRY(cudaStreamSynchronize(s->st));
+    s->n_set = s->u_set = true;
+    s->moments_fresh = true;
+    return SCLBM_OK;
+}
+
+int sclbm_reductions(sclbm_sim *s, double *mass, double *momentum) {
+    if (!s) return fail(SCLBM_ERR_ARG, "null handle");
+    if (!s->pop_set) return fail(SCLBM_ERR_STATE, "populations are not initialized");
+    DevGuard dg(s->device);
+    const int nv = 1 + s->D;
+    if (s->D == 2) {
+        if (s->fp32) k_reduce_pop<D2Q9, float><<<s->red_blocks, RED_THREADS, 0, s->st>>>((const float *)s->pop[s->cur], s->V, s->rho0, s->red);
+        else k_reduce_pop<D2Q9, double><<<s->red_blocks, RED_THREADS, 0, s->st>>>((const double *)s->pop[s->cur], s->V, 0.0, s->red);
+    } else {
+        if (s->fp32) k_reduce_pop<D3Q19, float><<<s->red_blocks, RED_THREADS, 0, s->st>>>((const float *)s->pop[s->cur], s->V, s->rho0, s->red);
+        else k_reduce_pop<D3Q19, double><<<s->red_blocks, RED_THREADS, 0, s->st>>>((const double *)s->pop[s->cur], s->V, 0.0, s->red);
+    }
+    std::vector<double> part;
+    int rc = finish_partials(s, nv, part);
+    if (rc) return rc;
+    double acc[4] = {0, 0, 0, 0};
+    for (int b = 0; b < s->red_blocks; b++)
+        for (int i = 0; i < nv; i++) acc[i] += part[(size_t)b * nv + i];
+    if (mass) *mass = acc[0];
+    if (momentum)
+        for (int d = 0; d < s->D; d++) momentum[d] = acc[1 + d];
+    return SCLBM_OK;
+}
+
+int sclbm_check_u(sclbm_sim *s, double *u_conv, double *max_u) {
+    if (!s) return fail(SCLBM_ERR_ARG, "null handle");
+    if (!s->moments_fresh) return fail(SCLBM_ERR_STATE, "call sclbm_compute_moments first");
+    DevGuard dg(s->device);
+    if (s->fp32) k_check_u<float><<<s->red_blocks, RED_THREADS, 0, s->st>>>((const float *)s->u, (float *)s->u_old, s->D, s->V, s->red);
+    else k_check_u<double><<<s->red_blocks, RED_THREADS, 0, s->st>>>((const double *)s->u, (double *)s->u_old, s->D, s->V, s->red);
+    std::vector<double> part;
+    int rc = finish_partials(s, 2, part);
+    if (rc) return rc;
+    double sum = 0, mx = 0;
+    for (int b = 0; b < s->red_blocks; b++) {
+        sum += part[(size_t)b * 2];
+        mx = std::max(mx, part[(size_t)b * 2 + 1]);
+    }
+    if (u_conv) *u_conv = sum / (double)s->V;
+    if (max_u) *max_u = std::sqrt(mx / s->c2);
+    return SCLBM_OK;
+}
+
+int sclbm_center_of_mass(sclbm_sim *s, double *mass, double *cm) {
+    if (!s) return fail(SCLBM_ERR_ARG, "null handle");
+    DevGuard dg(s->device);
+    if (s->fp32) k_com<float><<<s->red_blocks, RED_THREADS, 0, s->st>>>((const float *)s->dn, s->rho0, s->D, s->L[0], s->L[1], s->V, s->red);
+    else k_com<double><<<s->red_blocks, RED_THREADS, 0, s->st>>>((const double *)s->dn, 0.0, s->D, s->L[0], s->L[1], s->V, s->red);
+    std::vector<double> part;
+    int rc = finish_partials(s, 4, part);
+    if (rc) return rc;
+    double acc[4] = {0, 0, 0, 0};
+    for (int b = 0; b < s->red_blocks; b++)
+        for (int i = 0; i < 4; i++) acc[i] += part[(size_t)b * 4 + i];
+    if (mass) *mass = acc[0];
+    if (cm)
+        for (int d = 0; d < s->D; d++) cm[d] = acc[1 + d] / acc[0];
+    return SCLBM_OK;
+}
+
+int sclbm_density_at(sclbm_sim *s, const int64_t *idx, int count, double *out) {
+    if (!s || !idx || !out || count < 0) return fail(SCLBM_ERR_ARG, "bad argument");
+    DevGuard dg(s->device);
+    for (int i = 0; i < count; i++) {
+        if (idx[i] < 0 || idx[i] >= s->V) return fail(SCLBM_ERR_ARG, "index %lld out of range", (long long)idx[i]);
+        if (s->fp32) {
+            float v;
+            CUDA_TRY(cudaMemcpyAsync(&v, (const float *)s->dn + idx[i], 4, cudaMemcpyDeviceToHost, s->st));
+            CUDA_TRY(cudaStreamSynchronize(s->st));
+            out[i] = (double)v + s->rho0;
+        } else {
+            CUDA_TRY(cudaMemcpyAsync(out + i, (const double *)s->dn + idx[i], 8, cudaMemcpyDeviceToHost, s->st));
+            CUDA_TRY(cudaStreamSynchronize(s->st));
+        }
+    }
+    return SCLBM_OK;
+}
+
+int sclbm_density_finite(sclbm_sim *s, int *finite, double *max_abs) {
+    if (!s) return fail(SCLBM_ERR_ARG, "null handle");
+    DevGuard dg(s->device);
+    if (s->fp32) k_finite<float><<<s->red_blocks, RED_THREADS, 0, s->st>>>((const float *)s->dn, s->rho0, s->V, s->red);
+    else k_finite<double><<<s->red_blocks, RED_THREADS, 0, s->st>>>((const double *)s->dn, 0.0, s->V, s->red);
+    std::vector<double> part;
+    int rc = finish_partials(s, 2, part);
+    if (rc) return rc;
+    double bad = 0, mx = 0;
+    for (int b = 0; b < s->red_blocks; b++) {
+        bad = std::max(bad, part[(size_t)b * 2]);
+        mx = std::max(mx, part[(size_t)b * 2 + 1]);
+    }
+    if (finite) *finite = bad > 0 ? 0 : 1;
+    if (max_abs) *max_abs = mx;
+    return SCLBM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,290 @@
+"""ctypes binding of libsclbm.so (include/sclbm.h).
+
+There is no CPU fallback: if the library cannot be loaded, or no sm_100-family
+GPU is present, every call raises.
+"""
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+from . import build as _build
+
+OK, ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA, ERR_STATE, ERR_NOMEM, ERR_NODEVICE = range(7)
+PSI_EXP_INV, PSI_ONE_MINUS_EXP, PSI_IDENTITY = 0, 1, 2
+COLL_BGK, COLL_MRT = 0, 1
+FP64, FP32_SHIFTED = 0, 1
+LIT_ROUND15, LIT_EXACT = 0, 1
+
+
+class SclbmError(RuntimeError):
+    def __init__(self, fn, status, message):
+        self.status = status
+        super().__init__('%s failed (%d: %s): %s' % (fn, status, _STATUS.get(status, '?'), message))
+
+
+_STATUS = {OK: 'ok', ERR_ARG: 'invalid argument', ERR_UNSUPPORTED: 'unsupported configuration',
+           ERR_CUDA: 'CUDA error', ERR_STATE: 'call out of order', ERR_NOMEM: 'out of device memory',
+           ERR_NODEVICE: 'no usable device'}
+
+
+class Params(ctypes.Structure):
+    _fields_ = [('dim', ctypes.c_int), ('sizes', ctypes.c_int * 3), ('q', ctypes.c_int),
+                ('xi', ctypes.c_void_p), ('w', ctypes.c_void_p), ('c2', ctypes.c_double),
+                ('qe', ctypes.c_int), ('e', ctypes.c_void_p), ('we', ctypes.c_void_p),
+                ('sc_g', ctypes.c_double), ('psi_kind', ctypes.c_int), ('collision', ctypes.c_int),
+                ('tau', ctypes.c_double), ('mrt_s', ctypes.c_void_p), ('precision', ctypes.c_int),
+                ('rho0', ctypes.c_double), ('literals', ctypes.c_int), ('device', ctypes.c_int),
+                ('coll_a', ctypes.c_void_p), ('coll_b', ctypes.c_void_p)]
+
+
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_D = ctypes.c_double
+_DP = ctypes.POINTER(ctypes.c_double)
+_IP = ctypes.POINTER(ctypes.c_int)
+_I64P = ctypes.POINTER(ctypes.c_int64)
+
+# name -> argtypes (all return int unless listed in _STR)
+SIGNATURES = {
+    'sclbm_monomial_count': [ctypes.c_int],
+    'sclbm_version': [],
+    'sclbm_status_string': [ctypes.c_int],
+    'sclbm_last_error': [],
+    'sclbm_create': [ctypes.POINTER(Params), ctypes.POINTER(_P)],
+    'sclbm_destroy': [_P],
+    'sclbm_info': [_P, _I64P, _I64P],
+    'sclbm_set_density': [_P, _P],
+    'sclbm_set_velocity': [_P, _P],
+    'sclbm_get_density': [_P, _P],
+    'sclbm_get_velocity': [_P, _P],
+    'sclbm_get_populations': [_P, _P],
+    'sclbm_set_populations': [_P, _P],
+    'sclbm_set_collision': [_P, ctypes.c_int, _D, _P, _P, _P],
+    'sclbm_init_populations': [_P],
+    'sclbm_init_radial': [_P, _D, _D, _D, ctypes.c_int],
+    'sclbm_init_flat': [_P, _D, _D, _D, ctypes.c_int, ctypes.c_int],
+    'sclbm_init_single_flat': [_P, _D, _D, ctypes.c_int, ctypes.c_int],
+    'sclbm_init_cylinder': [_P, _D, _D, _D, ctypes.c_int, ctypes.c_int],
+    'sclbm_step': [_P, _I64],
+    'sclbm_sync': [_P],
+    'sclbm_step_timed': [_P, _I64, _DP],
+    'sclbm_profile_step': [_P, _I64, _DP, ctypes.c_int],
+    'sclbm_kernels_per_step': [_P, _IP],
+    'sclbm_compute_moments': [_P],
+    'sclbm_reductions': [_P, _DP, _DP],
+    'sclbm_check_u': [_P, _DP, _DP],
+    'sclbm_center_of_mass': [_P, _DP, _DP],
+    'sclbm_density_at': [_P, _I64P, ctypes.c_int, _DP],
+    'sclbm_density_finite': [_P, _IP, _DP],
+}
+_STR = {'sclbm_version', 'sclbm_status_string', 'sclbm_last_error'}
+
+_lock = threading.Lock()
+_lib = None
+
+
+def library_path():
+    return _build.LIB
+
+
+def load(build_if_missing=True):
+    """Load libsclbm.so (building it with nvcc if it is missing)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = _build.LIB
+        if not os.path.exists(path) and build_if_missing:
+            _build.build()
+        if not os.path.exists(path):
+            raise ImportError('libsclbm.so not built (%s); run __graft_entry__.build()' % path)
+        lib = ctypes.CDLL(path)
+        for name, args in SIGNATURES.items():
+            fn = getattr(lib, name)
+            fn.argtypes = args
+            fn.restype = ctypes.c_char_p if name in _STR else ctypes.c_int
+        _lib = lib
+        return lib
+
+
+def call(name, *args):
+    lib = load()
+    rc = getattr(lib, name)(*args)
+    if rc != OK:
+        raise SclbmError(name, rc, lib.sclbm_last_error().decode())
+    return rc
+
+
+def ptr(a):
+    return ctypes.c_void_p(a.ctypes.data)
+
+
+def dptr(a):
+    return a.ctypes.data_as(_DP)
+
+
+class Sim:
+    """Owning wrapper of one sclbm_sim handle."""
+
+    def __init__(self, dim, sizes, xi, w, c2, e, we, G, psi_kind=PSI_EXP_INV, collision=COLL_BGK,
+                 tau=1.0, mrt_s=None, precision=FP64, rho0=0.0, literals=LIT_ROUND15, device=0,
+                 coll_a=None, coll_b=None):
+        self.dim = int(dim)
+        self.sizes = tuple(int(s) for s in sizes)
+        self.q = len(xi)
+        self.V = int(np.prod(self.sizes))
+        self._xi = np.ascontiguousarray(np.array(xi, np.int32).ravel())
+        self._w = np.ascontiguousarray(np.array(w, np.float64))
+        self._e = np.ascontiguousarray(np.array(e, np.int32).ravel())
+        self._we = np.ascontiguousarray(np.array(we, np.float64))
+        p = Params()
+        p.dim = self.dim
+        for d in range(3):
+            p.sizes[d] = self.sizes[d] if d < self.dim else 1
+        p.q = self.q
+        p.xi, p.w, p.c2 = ptr(self._xi), ptr(self._w), float(c2)
+        p.qe, p.e, p.we = len(we), ptr(self._e), ptr(self._we)
+        p.sc_g, p.psi_kind, p.collision, p.tau = float(G), int(psi_kind), int(collision), float(tau)
+        self._keep = []
+        p.mrt_s = self._arr(mrt_s)
+        p.precision, p.rho0, p.literals, p.device = int(precision), float(rho0), int(literals), int(device)
+        p.coll_a, p.coll_b = self._arr(coll_a), self._arr(coll_b)
+        self.precision = int(precision)
+        h = ctypes.c_void_p()
+        call('sclbm_create', ctypes.byref(p), ctypes.byref(h))
+        self.h = h
+
+    def _arr(self, a):
+        if a is None:
+            return None
+        a = np.ascontiguousarray(np.asarray(a, np.float64))
+        self._keep.append(a)
+        return ptr(a)
+
+    def close(self):
+        if getattr(self, 'h', None):
+            load().sclbm_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # fields ---------------------------------------------------------------
+    def set_density(self, n):
+        n = np.ascontiguousarray(np.asarray(n, np.float64).ravel())
+        assert n.size == self.V
+        call('sclbm_set_density', self.h, ptr(n))
+
+    def set_velocity(self, u):
+        u = np.ascontiguousarray(np.asarray(u, np.float64).ravel())
+        assert u.size == self.V * self.dim
+        call('sclbm_set_velocity', self.h, ptr(u))
+
+    def get_density(self):
+        out = np.empty(self.V)
+        call('sclbm_get_density', self.h, ptr(out))
+        return out
+
+    def get_velocity(self):
+        out = np.empty(self.V * self.dim)
+        call('sclbm_get_velocity', self.h, ptr(out))
+        return out
+
+    def get_populations(self):
+        out = np.empty(self.V * self.q)
+        call('sclbm_get_populations', self.h, ptr(out))
+        return out
+
+    def set_populations(self, pop):
+        pop = np.ascontiguousarray(np.asarray(pop, np.float64).ravel())
+        assert pop.size == self.V * self.q
+        call('sclbm_set_populations', self.h, ptr(pop))
+
+    def set_collision(self, collision, tau=1.0, mrt_s=None, coll_a=None, coll_b=None):
+        call('sclbm_set_collision', self.h, int(collision), float(tau), self._arr(mrt_s),
+             self._arr(coll_a), self._arr(coll_b))
+
+    # init / step --------------------------------------------------------------
+    def init_populations(self):
+        call('sclbm_init_populations', self.h)
+
+    def init_radial(self, n_g, n_l, R, full_flag=True):
+        call('sclbm_init_radial', self.h, n_g, n_l, R, int(bool(full_flag)))
+
+    def init_flat(self, n_g, n_l, width, direction=0, full_flag=True):
+        call('sclbm_init_flat', self.h, n_g, n_l, width, int(direction), int(bool(full_flag)))
+
+    def init_single_flat(self, n_g, n_l, direction=0, full_flag=True):
+        call('sclbm_init_single_flat', self.h, n_g, n_l, int(direction), int(bool(full_flag)))
+
+    def init_cylinder(self, n_g, n_l, R, direction=0, full_flag=True):
+        call('sclbm_init_cylinder', self.h, n_g, n_l, R, int(direction), int(bool(full_flag)))
+
+    def step(self, nsteps, sync=True):
+        call('sclbm_step', self.h, int(nsteps))
+        if sync:
+            call('sclbm_sync', self.h)
+
+    def sync(self):
+        call('sclbm_sync', self.h)
+
+    def step_timed(self, nsteps):
+        ms = ctypes.c_double()
+        call('sclbm_step_timed', self.h, int(nsteps), ctypes.byref(ms))
+        return ms.value
+
+    def profile_step(self, nsteps):
+        ms = (ctypes.c_double * 2)()
+        call('sclbm_profile_step', self.h, int(nsteps), ms, 2)
+        return ms[0], ms[1]
+
+    def kernels_per_step(self):
+        c = ctypes.c_int()
+        call('sclbm_kernels_per_step', self.h, ctypes.byref(c))
+        return c.value
+
+    def info(self):
+        v, b = ctypes.c_int64(), ctypes.c_int64()
+        call('sclbm_info', self.h, ctypes.byref(v), ctypes.byref(b))
+        return v.value, b.value
+
+    # observables -------------------------------------------------------------
+    def compute_moments(self):
+        call('sclbm_compute_moments', self.h)
+
+    def reductions(self):
+        m = ctypes.c_double()
+        mom = (ctypes.c_double * 3)()
+        call('sclbm_reductions', self.h, ctypes.byref(m), mom)
+        return m.value, np.array(mom[:self.dim])
+
+    def check_u(self):
+        a, b = ctypes.c_double(), ctypes.c_double()
+        call('sclbm_check_u', self.h, ctypes.byref(a), ctypes.byref(b))
+        return a.value, b.value
+
+    def center_of_mass(self):
+        m = ctypes.c_double()
+        cm = (ctypes.c_double * 3)()
+        call('sclbm_center_of_mass', self.h, ctypes.byref(m), cm)
+        return m.value, tuple(cm[:self.dim])
+
+    def density_at(self, idx):
+        idx = np.ascontiguousarray(np.asarray(idx, np.int64).ravel())
+        out = np.empty(idx.size)
+        call('sclbm_density_at', self.h, idx.ctypes.data_as(_I64P), int(idx.size), dptr(out))
+        return out
+
+    def density_finite(self):
+        f, m = ctypes.c_int(), ctypes.c_double()
+        call('sclbm_density_finite', self.h, ctypes.byref(f), ctypes.byref(m))
+        return bool(f.value), m.value
+
+
+def monomial_count(dim):
+    return load().sclbm_monomial_count(int(dim))

@@ -42,6 +42,12 @@
 
 #include <stdint.h>
 
+#if defined(__GNUC__)
+#define SCLBM_API __attribute__((visibility("default")))
+#else
+#define SCLBM_API
+#endif
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -94,67 +100,83 @@ typedef struct sclbm_params {
     double rho0;               /* FP32_SHIFTED: reference density of the shift */
     int literals;              /* SCLBM_LIT_* (FP64 path) */
     int device;                /* CUDA device ordinal */
+    /* Optional explicit collision operator, overriding the one built from tau /
+     * mrt_s: f*_q = sum_j coll_a[q*q+j] f_j + sum_k coll_b[q*K+k] m_k over the
+     * K = sclbm_monomial_count(dim) monomials
+     *   [n, n u_a, n u_a u_b (a<=b), F_a, F_a u_b]
+     * (how a specific generated reference kernel's printed literals are
+     * reproduced exactly).  Both null, or both set. */
+    const double *coll_a;
+    const double *coll_b;
 } sclbm_params;
 
+/* number of collision monomials for a dimension (12 in 2D, 22 in 3D) */
+SCLBM_API int sclbm_monomial_count(int dim);
+
 /* library */
-const char *sclbm_version(void);
-const char *sclbm_status_string(int status);
+SCLBM_API const char *sclbm_version(void);
+SCLBM_API const char *sclbm_status_string(int status);
 /* message of the last failed call on this thread (empty if none) */
-const char *sclbm_last_error(void);
+SCLBM_API const char *sclbm_last_error(void);
 
 /* lifetime */
-int sclbm_create(const sclbm_params *p, sclbm_sim **out);
-int sclbm_destroy(sclbm_sim *s);
+SCLBM_API int sclbm_create(const sclbm_params *p, sclbm_sim **out);
+SCLBM_API int sclbm_destroy(sclbm_sim *s);
 
 /* lattice volume and the footprint of the handle in device memory */
-int sclbm_info(const sclbm_sim *s, int64_t *volume, int64_t *device_bytes);
+SCLBM_API int sclbm_info(const sclbm_sim *s, int64_t *volume, int64_t *device_bytes);
 
 /* fields; host arrays are FP64, x fastest; u as dim planes of volume values */
-int sclbm_set_density(sclbm_sim *s, const double *n);
-int sclbm_set_velocity(sclbm_sim *s, const double *u);
-int sclbm_get_density(sclbm_sim *s, double *n);
-int sclbm_get_velocity(sclbm_sim *s, double *u);
+SCLBM_API int sclbm_set_density(sclbm_sim *s, const double *n);
+SCLBM_API int sclbm_set_velocity(sclbm_sim *s, const double *u);
+SCLBM_API int sclbm_get_density(sclbm_sim *s, double *n);
+SCLBM_API int sclbm_get_velocity(sclbm_sim *s, double *u);
 /* populations as q planes of volume values (f_q, not the FP32 deviations) */
-int sclbm_get_populations(sclbm_sim *s, double *pop);
-int sclbm_set_populations(sclbm_sim *s, const double *pop);
+SCLBM_API int sclbm_get_populations(sclbm_sim *s, double *pop);
+SCLBM_API int sclbm_set_populations(sclbm_sim *s, const double *pop);
+
+/* replace the collision operator (MainLoop <-> MainLoopMRT switch); the
+ * populations are kept.  Arguments as the sclbm_params fields of the same name. */
+SCLBM_API int sclbm_set_collision(sclbm_sim *s, int collision, double tau, const double *mrt_s,
+                                  const double *coll_a, const double *coll_b);
 
 /* initialisation */
-int sclbm_init_populations(sclbm_sim *s);
-int sclbm_init_radial(sclbm_sim *s, double n_g, double n_l, double R, int full_flag);
-int sclbm_init_flat(sclbm_sim *s, double n_g, double n_l, double width, int direction,
+SCLBM_API int sclbm_init_populations(sclbm_sim *s);
+SCLBM_API int sclbm_init_radial(sclbm_sim *s, double n_g, double n_l, double R, int full_flag);
+SCLBM_API int sclbm_init_flat(sclbm_sim *s, double n_g, double n_l, double width, int direction,
                     int full_flag);
-int sclbm_init_single_flat(sclbm_sim *s, double n_g, double n_l, int direction, int full_flag);
-int sclbm_init_cylinder(sclbm_sim *s, double n_g, double n_l, double R, int direction,
+SCLBM_API int sclbm_init_single_flat(sclbm_sim *s, double n_g, double n_l, int direction, int full_flag);
+SCLBM_API int sclbm_init_cylinder(sclbm_sim *s, double n_g, double n_l, double R, int direction,
                         int full_flag);
 
 /* time stepping: enqueue nsteps steps on the handle's stream (returns without
  * waiting); sclbm_sync waits for everything enqueued on the handle */
-int sclbm_step(sclbm_sim *s, int64_t nsteps);
-int sclbm_sync(sclbm_sim *s);
+SCLBM_API int sclbm_step(sclbm_sim *s, int64_t nsteps);
+SCLBM_API int sclbm_sync(sclbm_sim *s);
 /* as sclbm_step, bracketed by CUDA events on the handle's stream; waits and
  * returns the elapsed device time in milliseconds */
-int sclbm_step_timed(sclbm_sim *s, int64_t nsteps, double *ms);
+SCLBM_API int sclbm_step_timed(sclbm_sim *s, int64_t nsteps, double *ms);
 /* per-kernel device time of one step, averaged over nsteps (ms[0]: density+psi
  * pass, ms[1]: fused force+collide+stream pass); kernels are launched one by
  * one, each bracketed by events */
-int sclbm_profile_step(sclbm_sim *s, int64_t nsteps, double *ms, int nms);
+SCLBM_API int sclbm_profile_step(sclbm_sim *s, int64_t nsteps, double *ms, int nms);
 /* count of kernels launched by sclbm_step per lattice step */
-int sclbm_kernels_per_step(const sclbm_sim *s, int *count);
+SCLBM_API int sclbm_kernels_per_step(const sclbm_sim *s, int *count);
 
 /* observables */
-int sclbm_compute_moments(sclbm_sim *s);
+SCLBM_API int sclbm_compute_moments(sclbm_sim *s);
 /* sum of all populations (FP64 accumulation) and total momentum sum_q xi_q f_q */
-int sclbm_reductions(sclbm_sim *s, double *mass, double *momentum);
+SCLBM_API int sclbm_reductions(sclbm_sim *s, double *mass, double *momentum);
 /* CheckUConvergenceSCMP on the last compute_moments velocity:
  * u_conv = sum_cells sum_d |u - u_old| / V, max_u = sqrt(max |u|^2 / c2); then
  * u_old = u.  The first call compares against zero, as the reference does. */
-int sclbm_check_u(sclbm_sim *s, double *u_conv, double *max_u);
+SCLBM_API int sclbm_check_u(sclbm_sim *s, double *u_conv, double *max_u);
 /* mass and centre of mass sum(n x_d)/sum(n) from the density field */
-int sclbm_center_of_mass(sclbm_sim *s, double *mass, double *cm);
+SCLBM_API int sclbm_center_of_mass(sclbm_sim *s, double *mass, double *cm);
 /* density at count linear cell indices */
-int sclbm_density_at(sclbm_sim *s, const int64_t *idx, int count, double *out);
+SCLBM_API int sclbm_density_at(sclbm_sim *s, const int64_t *idx, int count, double *out);
 /* 1 if every density value is finite, else 0 (max |n| also returned) */
-int sclbm_density_finite(sclbm_sim *s, int *finite, double *max_abs);
+SCLBM_API int sclbm_density_finite(sclbm_sim *s, int *finite, double *max_abs);
 
 #ifdef __cplusplus
 }
