@@ -1,0 +1,6 @@
+// D3Q19 + E4 kernels, FP64, fused arithmetic (BGK and MRT).
+#include "launch.cuh"
+
+namespace sclbm {
+SCLBM_OPS_TU(ops_d3q19_e4_f64, D3Q19, D3E4, double, false)
+}  // namespace sclbm

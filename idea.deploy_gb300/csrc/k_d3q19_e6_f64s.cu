@@ -1,0 +1,6 @@
+// D3Q19 + E6 kernels, FP64, reference arithmetic (BGK and MRT).
+#include "launch.cuh"
+
+namespace sclbm {
+SCLBM_OPS_TU(ops_d3q19_e6_f64s, D3Q19, D3E6, double, true)
+}  // namespace sclbm

@@ -96,6 +96,15 @@ __device__ __forceinline__ int64_t index_at(const Cell<D> &c, int dx, int dy, in
     return (int64_t)x + (int64_t)Ls[0] * (y + (int64_t)Ls[1] * z);
 }
 
+// population i of the reference's summation order: its generated C names them
+// pop_0 .. pop_{Q-1} and sympy prints sums sorted by name ('pop_10' < 'pop_2')
+template <int Q>
+SCLBM_HD constexpr int lex_q(int i) {
+    if (Q <= 10) return i;
+    constexpr int t19[19] = {0, 1, 10, 11, 12, 13, 14, 15, 16, 17, 18, 2, 3, 4, 5, 6, 7, 8, 9};
+    return t19[i];
+}
+
 // ---------------------------------------------------------------------------
 // pass 1: density (deviation) and pseudopotential
 // ---------------------------------------------------------------------------
@@ -105,9 +114,10 @@ __global__ void __launch_bounds__(256) k_density_psi(const Real *__restrict__ po
                                                     int psi_kind) {
     const int64_t V = geo.V;
     for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < V; g += (int64_t)gridDim.x * blockDim.x) {
-        Real s = pop[g];
+        // summed in the reference's order (plain adds are never reassociated)
+        Real s = pop[(int64_t)lex_q<L::Q>(0) * V + g];
 #pragma unroll
-        for (int q = 1; q < L::Q; q++) s += pop[(int64_t)q * V + g];
+        for (int i = 1; i < L::Q; i++) s += pop[(int64_t)lex_q<L::Q>(i) * V + g];
         dn[g] = s;
         psi[g] = psi_of<Real>(psi_kind, rho0 + s);
     }
@@ -131,6 +141,103 @@ __device__ __forceinline__ void sc_force(const Real *__restrict__ psi, const Cel
     const Real s = p.neg_g * __ldg(psi + g);
 #pragma unroll
     for (int d = 0; d < D; d++) F[d] *= s;
+}
+
+// ---------------------------------------------------------------------------
+// Reference arithmetic (FP64, SCLBM_LIT_ROUND15): every sum in the order the
+// reference's generated C evaluates it (sympy prints terms sorted by name, so
+// 'pop_10' precedes 'pop_2'), every product associated left to right, and no
+// contraction into FMA (__dadd_rn / __dmul_rn are never fused).  With the
+// same literals, the only remaining difference to the reference is the libm
+// exp() of the pseudopotential.
+// ---------------------------------------------------------------------------
+template <class L>
+__device__ __forceinline__ double strict_density(const double *f) {
+    double s = f[lex_q<L::Q>(0)];
+#pragma unroll
+    for (int i = 1; i < L::Q; i++) s = __dadd_rn(s, f[lex_q<L::Q>(i)]);
+    return s;
+}
+
+template <class L, class S, class P>
+__device__ __forceinline__ void strict_force(const double *__restrict__ psi, const Cell<L::D> &c, int64_t g,
+                                             const P &p, double *F) {
+    constexpr int D = L::D;
+#pragma unroll
+    for (int d = 0; d < D; d++) F[d] = 0.0;
+#pragma unroll
+    for (int a = 0; a < S::QE; a++) {
+        const int64_t nb = index_at<D>(c, S::e(a, 0), S::e(a, 1), D == 3 ? S::e(a, 2) : 0, p.geo.L);
+        const double ps = __ldg(psi + nb);
+#pragma unroll
+        for (int d = 0; d < D; d++) {
+            if (S::e(a, d) == 0) continue;
+            const double t = __dmul_rn(fabs(p.sw[a][d]), ps);
+            F[d] = S::e(a, d) > 0 ? __dadd_rn(F[d], t) : __dsub_rn(F[d], t);
+        }
+    }
+    const double s = __dmul_rn(p.neg_g, __ldg(psi + g));
+#pragma unroll
+    for (int d = 0; d < D; d++) F[d] = __dmul_rn(F[d], s);
+}
+
+template <class L>
+__device__ __forceinline__ void strict_velocity(const double *f, double n, const double *F, double *u) {
+    constexpr int D = L::D;
+#pragma unroll
+    for (int d = 0; d < D; d++) {
+        double j = 0.0;
+        bool first = true;
+#pragma unroll
+        for (int i = 0; i < L::Q; i++) {
+            const int q = lex_q<L::Q>(i);
+            const int x = L::xi(q, d);
+            if (x == 0) continue;
+            if (first) j = x > 0 ? f[q] : -f[q];
+            else j = x > 0 ? __dadd_rn(j, f[q]) : __dsub_rn(j, f[q]);
+            first = false;
+        }
+        u[d] = __dadd_rn(__ddiv_rn(j, n), __ddiv_rn(__dmul_rn(0.5, F[d]), n));
+    }
+}
+
+// one term of the expanded collision, reference association ((c*x1)*x2)*x3
+template <int D>
+__device__ __forceinline__ double strict_term(int k, double c, double n, const double *u, const double *F) {
+    using M = Mono<D>;
+    if (k == 0) return __dmul_rn(c, n);
+    if (k < M::NUU) return __dmul_rn(__dmul_rn(c, n), u[k - M::NU]);
+    if (k < M::F) {
+#pragma unroll
+        for (int a = 0; a < D; a++)
+#pragma unroll
+            for (int b = a; b < D; b++)
+                if (M::nuu(a, b) == k) return __dmul_rn(__dmul_rn(__dmul_rn(c, n), u[a]), u[b]);
+        return 0.0;
+    }
+    if (k < M::FU) return __dmul_rn(c, F[k - M::F]);
+    const int a = (k - M::FU) / D, b = (k - M::FU) % D;
+    return __dmul_rn(__dmul_rn(c, F[a]), u[b]);
+}
+
+// monomials in the reference's print order: d_psi_a (then d_psi_a*lu_0_b), ln_0,
+// ln_0*lu_0_a (then ln_0*lu_0_a*lu_0_b, b >= a)
+template <int D>
+SCLBM_HD constexpr int print_order(int i) {
+    using M = Mono<D>;
+    int pos = 0;
+    for (int a = 0; a < D; a++) {
+        if (pos++ == i) return M::F + a;
+        for (int b = 0; b < D; b++)
+            if (pos++ == i) return M::FU + a * D + b;
+    }
+    if (pos++ == i) return 0;
+    for (int a = 0; a < D; a++) {
+        if (pos++ == i) return M::NU + a;
+        for (int b = a; b < D; b++)
+            if (pos++ == i) return M::nuu(a, b);
+    }
+    return -1;
 }
 
 // Guo-shifted velocity: u = (sum_q xi_q f_q + F/2) / n
@@ -171,40 +278,81 @@ __device__ __forceinline__ void monomials(Real dn, Real n, const Real *u, const 
 // ---------------------------------------------------------------------------
 // pass 2: force + collision + push stream
 // ---------------------------------------------------------------------------
-template <class L, class S, bool MRT, class Real>
+template <class L, class S, bool MRT, class Real, bool STRICT>
+__device__ __forceinline__ void collide_cell(const Real *f, Real d, Real n, const Real *u, const Real *F, int q,
+                                             const StepParams<L, S, Real> &p, Real &out) {
+    constexpr int D = L::D, Q = L::Q, K = Mono<D>::K;
+    if constexpr (STRICT) {
+        // reference order: monomial terms, then the population terms
+        double acc = 0.0;
+#pragma unroll
+        for (int i = 0; i < K; i++) {
+            const int k = print_order<D>(i);
+            if (!MRT && !bgk_nonzero<L>(q, k)) continue;
+            acc = __dadd_rn(acc, strict_term<D>(k, p.B[q][k], d, u, F));
+        }
+        if (MRT) {
+#pragma unroll
+            for (int i = 0; i < Q; i++) {
+                const int j = lex_q<Q>(i);
+                acc = __dadd_rn(acc, __dmul_rn(p.A[q][j], f[j]));
+            }
+        } else if (p.a_nonzero) {
+            acc = __dadd_rn(acc, __dmul_rn(p.A[q][q], f[q]));
+        }
+        out = acc;
+    } else {
+        Real m[K];
+        monomials<D, Real>(d, n, u, F, m);
+        Real acc = Real(0);
+        if (MRT) {
+#pragma unroll
+            for (int j = 0; j < Q; j++) acc = fma(p.A[q][j], f[j], acc);
+        } else if (p.a_nonzero) {
+            acc = p.A[q][q] * f[q];
+        }
+#pragma unroll
+        for (int k = 0; k < K; k++)
+            if (MRT || bgk_nonzero<L>(q, k)) acc = fma(p.B[q][k], m[k], acc);
+        out = acc;
+    }
+}
+
+template <class L, class S, class Real, bool STRICT>
+__device__ __forceinline__ void force_velocity(const Real *__restrict__ psi, const Cell<L::D> &c, int64_t g,
+                                               const StepParams<L, S, Real> &p, const Real *f, Real n, Real *F,
+                                               Real *u) {
+    if constexpr (STRICT) {
+        strict_force<L, S>(psi, c, g, p, F);
+        strict_velocity<L>(f, n, F, u);
+    } else {
+        sc_force<L, S, Real>(psi, c, g, p, F);
+        velocity<L, Real>(f, n, F, u);
+    }
+}
+
+template <class L, class S, bool MRT, class Real, bool STRICT>
 __global__ void __launch_bounds__(128) k_fcs(const Real *__restrict__ pop, Real *__restrict__ pop_out,
                                             const Real *__restrict__ dn, const Real *__restrict__ psi,
                                             const __grid_constant__ StepParams<L, S, Real> p) {
-    constexpr int D = L::D, Q = L::Q, K = Mono<D>::K;
+    constexpr int D = L::D, Q = L::Q;
     const int64_t V = p.geo.V;
     for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < V; g += (int64_t)gridDim.x * blockDim.x) {
         Cell<D> c;
         cell_of<D>(g, p.geo.L, c);
-        Real F[D];
-        sc_force<L, S, Real>(psi, c, g, p, F);
         Real f[Q];
 #pragma unroll
         for (int q = 0; q < Q; q++) f[q] = __ldg(pop + (int64_t)q * V + g);
         const Real d = __ldg(dn + g);
         const Real n = p.rho0 + d;
-        Real u[D];
-        velocity<L, Real>(f, n, F, u);
-        Real m[K];
-        monomials<D, Real>(d, n, u, F, m);
+        Real F[D], u[D];
+        force_velocity<L, S, Real, STRICT>(psi, c, g, p, f, n, F, u);
 #pragma unroll
         for (int q = 0; q < Q; q++) {
-            Real acc = Real(0);
-            if (MRT) {
-#pragma unroll
-                for (int j = 0; j < Q; j++) acc = fma(p.A[q][j], f[j], acc);
-            } else if (p.a_nonzero) {
-                acc = p.A[q][q] * f[q];
-            }
-#pragma unroll
-            for (int k = 0; k < K; k++)
-                if (MRT || bgk_nonzero<L>(q, k)) acc = fma(p.B[q][k], m[k], acc);
+            Real out;
+            collide_cell<L, S, MRT, Real, STRICT>(f, d, n, u, F, q, p, out);
             const int64_t dst = index_at<D>(c, L::xi(q, 0), L::xi(q, 1), D == 3 ? L::xi(q, 2) : 0, p.geo.L);
-            pop_out[(int64_t)q * V + dst] = acc;
+            pop_out[(int64_t)q * V + dst] = out;
         }
     }
 }
@@ -212,7 +360,7 @@ __global__ void __launch_bounds__(128) k_fcs(const Real *__restrict__ pop, Real 
 // ---------------------------------------------------------------------------
 // moments read-back: Guo-shifted velocity (and n) after the force
 // ---------------------------------------------------------------------------
-template <class L, class S, bool MRT, class Real>
+template <class L, class S, class Real, bool STRICT>
 __global__ void __launch_bounds__(128) k_velocity(const Real *__restrict__ pop, const Real *__restrict__ dn,
                                                  const Real *__restrict__ psi, Real *__restrict__ u_out,
                                                  const __grid_constant__ StepParams<L, S, Real> p) {
@@ -221,14 +369,12 @@ __global__ void __launch_bounds__(128) k_velocity(const Real *__restrict__ pop, 
     for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < V; g += (int64_t)gridDim.x * blockDim.x) {
         Cell<D> c;
         cell_of<D>(g, p.geo.L, c);
-        Real F[D];
-        sc_force<L, S, Real>(psi, c, g, p, F);
         Real f[Q];
 #pragma unroll
         for (int q = 0; q < Q; q++) f[q] = pop[(int64_t)q * V + g];
         const Real n = p.rho0 + dn[g];
-        Real u[D];
-        velocity<L, Real>(f, n, F, u);
+        Real F[D], u[D];
+        force_velocity<L, S, Real, STRICT>(psi, c, g, p, f, n, F, u);
 #pragma unroll
         for (int d = 0; d < D; d++) u_out[(int64_t)d * V + g] = u[d];
     }
@@ -237,7 +383,7 @@ __global__ void __launch_bounds__(128) k_velocity(const Real *__restrict__ pop, 
 // ---------------------------------------------------------------------------
 // equilibrium initialisation from (dn, u)
 // ---------------------------------------------------------------------------
-template <class L, class Real>
+template <class L, class Real, bool STRICT>
 __global__ void __launch_bounds__(128) k_init_pop(Real *__restrict__ pop, const Real *__restrict__ dn,
                                                  const Real *__restrict__ u_in,
                                                  const __grid_constant__ EqParams<L, Real> p) {
@@ -249,14 +395,38 @@ __global__ void __launch_bounds__(128) k_init_pop(Real *__restrict__ pop, const 
         Real u[D], F[D];
 #pragma unroll
         for (int a = 0; a < D; a++) { u[a] = u_in[(int64_t)a * V + g]; F[a] = Real(0); }
-        Real m[K];
-        monomials<D, Real>(d, n, u, F, m);
+        if constexpr (STRICT) {
+            // the reference forms n*u_a and n*u_a*u_b first, then multiplies by the literal
 #pragma unroll
-        for (int q = 0; q < Q; q++) {
-            Real acc = Real(0);
+            for (int q = 0; q < Q; q++) {
+                double acc = 0.0;
 #pragma unroll
-            for (int k = 0; k < Mono<D>::F; k++) acc = fma(p.B[q][k], m[k], acc);
-            pop[(int64_t)q * V + g] = acc;
+                for (int i = 0; i < K; i++) {
+                    const int k = print_order<D>(i);
+                    if (k >= Mono<D>::F) continue;
+                    double prod = d;
+                    if (k >= Mono<D>::NU && k < Mono<D>::NUU) prod = __dmul_rn(d, u[k - Mono<D>::NU]);
+                    if (k >= Mono<D>::NUU) {
+#pragma unroll
+                        for (int a = 0; a < D; a++)
+#pragma unroll
+                            for (int b = a; b < D; b++)
+                                if (Mono<D>::nuu(a, b) == k) prod = __dmul_rn(__dmul_rn(d, u[a]), u[b]);
+                    }
+                    acc = __dadd_rn(acc, __dmul_rn(p.B[q][k], prod));
+                }
+                pop[(int64_t)q * V + g] = acc;
+            }
+        } else {
+            Real m[K];
+            monomials<D, Real>(d, n, u, F, m);
+#pragma unroll
+            for (int q = 0; q < Q; q++) {
+                Real acc = Real(0);
+#pragma unroll
+                for (int k = 0; k < Mono<D>::F; k++) acc = fma(p.B[q][k], m[k], acc);
+                pop[(int64_t)q * V + g] = acc;
+            }
         }
     }
 }

@@ -43,7 +43,7 @@ struct KernelOps {
     void (*grids)(int sms, int *density_grid, int *fcs_grid);
 };
 
-template <class L, class S, bool MRT, class Real>
+template <class L, class S, bool MRT, class Real, bool STRICT>
 struct Ops {
     using SP = StepParams<L, S, Real>;
     using EP = EqParams<L, Real>;
@@ -85,18 +85,18 @@ struct Ops {
     }
     static cudaError_t fcs(const void *pop, void *pop_out, const void *dn, const void *psi, const void *sp, int grid,
                            cudaStream_t st) {
-        k_fcs<L, S, MRT, Real><<<grid, 128, 0, st>>>((const Real *)pop, (Real *)pop_out, (const Real *)dn,
+        k_fcs<L, S, MRT, Real, STRICT><<<grid, 128, 0, st>>>((const Real *)pop, (Real *)pop_out, (const Real *)dn,
                                                      (const Real *)psi, *static_cast<const SP *>(sp));
         return cudaGetLastError();
     }
     static cudaError_t velocity(const void *pop, const void *dn, const void *psi, void *u, const void *sp, int grid,
                                 cudaStream_t st) {
-        k_velocity<L, S, MRT, Real><<<grid, 128, 0, st>>>((const Real *)pop, (const Real *)dn, (const Real *)psi,
+        k_velocity<L, S, Real, STRICT><<<grid, 128, 0, st>>>((const Real *)pop, (const Real *)dn, (const Real *)psi,
                                                           (Real *)u, *static_cast<const SP *>(sp));
         return cudaGetLastError();
     }
     static cudaError_t init_pop(void *pop, const void *dn, const void *u, const void *ep, int grid, cudaStream_t st) {
-        k_init_pop<L, Real><<<grid, 128, 0, st>>>((Real *)pop, (const Real *)dn, (const Real *)u,
+        k_init_pop<L, Real, STRICT><<<grid, 128, 0, st>>>((Real *)pop, (const Real *)dn, (const Real *)u,
                                                   *static_cast<const EP *>(ep));
         return cudaGetLastError();
     }
@@ -105,7 +105,7 @@ struct Ops {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_density_psi<L, Real>, 256, 0);
         *dg = sms * (b > 0 ? b : 1);
         b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fcs<L, S, MRT, Real>, 128, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fcs<L, S, MRT, Real, STRICT>, 128, 0);
         *fg = sms * (b > 0 ? b : 1);
     }
     static const KernelOps *ops() {
@@ -115,10 +115,41 @@ struct Ops {
     }
 };
 
-// per translation unit: ops for (stencil order, collision, precision), or null
-const KernelOps *ops_d2q9(int order, bool mrt, bool fp32);
-const KernelOps *ops_d3q19_e4(bool mrt, bool fp32);
-const KernelOps *ops_d3q19_e6(bool mrt, bool fp32);
-const KernelOps *ops_d3q19_e8(bool mrt, bool fp32);
+// One translation unit per (lattice, stencil, precision/arithmetic) so that
+// the instantiations compile in parallel; each defines ops_<lat>_e<order>_<v>
+// (v: f32 = FP32-shifted, f64 = FP64 fused arithmetic, f64s = FP64 reference
+// arithmetic, i.e. the reference's evaluation order without FMA).
+#define SCLBM_OPS_TU(NAME, L, S, REAL, STRICT)                                                    \
+    const KernelOps *NAME(bool mrt) {                                                             \
+        return mrt ? Ops<L, S, true, REAL, STRICT>::ops() : Ops<L, S, false, REAL, STRICT>::ops(); \
+    }
+
+#define SCLBM_DECLARE_OPS(LAT)                                                                    \
+    const KernelOps *ops_##LAT##_e4_f32(bool);                                                    \
+    const KernelOps *ops_##LAT##_e4_f64(bool);                                                    \
+    const KernelOps *ops_##LAT##_e4_f64s(bool);                                                   \
+    const KernelOps *ops_##LAT##_e6_f32(bool);                                                    \
+    const KernelOps *ops_##LAT##_e6_f64(bool);                                                    \
+    const KernelOps *ops_##LAT##_e6_f64s(bool);                                                   \
+    const KernelOps *ops_##LAT##_e8_f32(bool);                                                    \
+    const KernelOps *ops_##LAT##_e8_f64(bool);                                                    \
+    const KernelOps *ops_##LAT##_e8_f64s(bool);
+SCLBM_DECLARE_OPS(d2q9)
+SCLBM_DECLARE_OPS(d3q19)
+
+// kernel set for (dimension, stencil order, collision, precision, arithmetic)
+inline const KernelOps *select_ops(int dim, int order, bool mrt, bool fp32, bool strict) {
+    using Fn = const KernelOps *(*)(bool);
+    static const Fn t2[3][3] = {{ops_d2q9_e4_f32, ops_d2q9_e4_f64, ops_d2q9_e4_f64s},
+                                {ops_d2q9_e6_f32, ops_d2q9_e6_f64, ops_d2q9_e6_f64s},
+                                {ops_d2q9_e8_f32, ops_d2q9_e8_f64, ops_d2q9_e8_f64s}};
+    static const Fn t3[3][3] = {{ops_d3q19_e4_f32, ops_d3q19_e4_f64, ops_d3q19_e4_f64s},
+                                {ops_d3q19_e6_f32, ops_d3q19_e6_f64, ops_d3q19_e6_f64s},
+                                {ops_d3q19_e8_f32, ops_d3q19_e8_f64, ops_d3q19_e8_f64s}};
+    const int o = order == 4 ? 0 : order == 6 ? 1 : order == 8 ? 2 : -1;
+    if (o < 0 || (dim != 2 && dim != 3)) return nullptr;
+    const int v = fp32 ? 0 : strict ? 2 : 1;
+    return (dim == 2 ? t2 : t3)[o][v](mrt);
+}
 
 }  // namespace sclbm

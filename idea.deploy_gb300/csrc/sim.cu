@@ -476,11 +476,9 @@ int configure(sclbm_sim *s, int collision, double tau, const double *mrt_s, cons
         t.B.assign(coll_b, coll_b + (size_t)s->Q * t.K);
     }
     const bool mrt = collision == SCLBM_COLL_MRT || coll_a != nullptr;
-    const KernelOps *ops = nullptr;
-    if (s->D == 2) ops = ops_d2q9(s->order, mrt, s->fp32);
-    else if (s->order == 4) ops = ops_d3q19_e4(mrt, s->fp32);
-    else if (s->order == 6) ops = ops_d3q19_e6(mrt, s->fp32);
-    else ops = ops_d3q19_e8(mrt, s->fp32);
+    // FP64 with the reference's literals also uses the reference's arithmetic
+    const bool strict = !s->fp32 && s->literals == SCLBM_LIT_ROUND15;
+    const KernelOps *ops = select_ops(s->D, s->order, mrt, s->fp32, strict);
     if (!ops) return fail(SCLBM_ERR_UNSUPPORTED, "no kernels for this configuration");
     bool a_nonzero = false;
     for (int q = 0; q < s->Q; q++) a_nonzero = a_nonzero || t.A[(size_t)q * s->Q + q] != 0.0;
