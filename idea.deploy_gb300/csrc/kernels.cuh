@@ -11,6 +11,7 @@
 
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <type_traits>
 
 #include "lattice.cuh"
 
@@ -347,12 +348,20 @@ __global__ void __launch_bounds__(128) k_fcs(const Real *__restrict__ pop, Real 
         const Real n = p.rho0 + d;
         Real F[D], u[D];
         force_velocity<L, S, Real, STRICT>(psi, c, g, p, f, n, F, u);
+        Real out[Q];
+#pragma unroll
+        for (int q = 0; q < Q; q++) collide_cell<L, S, MRT, Real, STRICT>(f, d, n, u, F, q, p, out[q]);
+        if constexpr (std::is_same<Real, float>::value) {
+            // FP32 storage: rest population from mass conservation (as the single-pass kernel)
+            Real rest = d;
+#pragma unroll
+            for (int q = 1; q < Q; q++) rest -= out[q];
+            out[0] = rest;
+        }
 #pragma unroll
         for (int q = 0; q < Q; q++) {
-            Real out;
-            collide_cell<L, S, MRT, Real, STRICT>(f, d, n, u, F, q, p, out);
             const int64_t dst = index_at<D>(c, L::xi(q, 0), L::xi(q, 1), D == 3 ? L::xi(q, 2) : 0, p.geo.L);
-            pop_out[(int64_t)q * V + dst] = out;
+            pop_out[(int64_t)q * V + dst] = out[q];
         }
     }
 }

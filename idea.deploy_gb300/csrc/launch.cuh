@@ -7,7 +7,9 @@
 #include <cstdint>
 #include <cstring>
 #include <cuda_runtime.h>
+#include <type_traits>
 
+#include "fused.cuh"
 #include "kernels.cuh"
 
 namespace sclbm {
@@ -41,6 +43,11 @@ struct KernelOps {
                             cudaStream_t st);
     // occupancy-derived grid sizes (blocks) for a device with `sms` SMs
     void (*grids)(int sms, int *density_grid, int *fcs_grid);
+    // single-pass step (FP32 only, else null): launcher, tile shape, resident CTAs per SM
+    cudaError_t (*fused)(const void *pop, void *pop_out, const void *step_params, const FusedGeom &fg, int grid,
+                         cudaStream_t st);
+    int fused_tx, fused_ty, fused_r;
+    int (*fused_occupancy)();
 };
 
 template <class L, class S, bool MRT, class Real, bool STRICT>
@@ -108,9 +115,32 @@ struct Ops {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fcs<L, S, MRT, Real, STRICT>, 128, 0);
         *fg = sms * (b > 0 ? b : 1);
     }
+    static cudaError_t fused(const void *pop, void *pop_out, const void *sp, const FusedGeom &fg, int grid,
+                             cudaStream_t st) {
+        if constexpr (std::is_same<Real, float>::value) {
+            using SH = FusedShape<L, S>;
+            k_fused<L, S, MRT><<<grid, SH::NT, SH::SMEM, st>>>((const float *)pop, (float *)pop_out,
+                                                               *static_cast<const SP *>(sp), fg);
+            return cudaGetLastError();
+        }
+        return cudaErrorNotSupported;
+    }
+    static int fused_occupancy() {
+        if constexpr (std::is_same<Real, float>::value) {
+            using SH = FusedShape<L, S>;
+            int b = 0;
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fused<L, S, MRT>, SH::NT, SH::SMEM);
+            return b > 0 ? b : 1;
+        }
+        return 0;
+    }
     static const KernelOps *ops() {
-        static const KernelOps o = {sizeof(SP), sizeof(EP), 2, &fill_step, &fill_eq, &density,
-                                    &fcs, &velocity, &init_pop, &grids};
+        constexpr bool f32 = std::is_same<Real, float>::value;
+        using SH = FusedShape<L, S>;
+        static const KernelOps o = {sizeof(SP), sizeof(EP), f32 ? 1 : 2, &fill_step, &fill_eq, &density,
+                                    &fcs, &velocity, &init_pop, &grids,
+                                    f32 ? &fused : nullptr, SH::TX, SH::TY, SH::R,
+                                    f32 ? &fused_occupancy : nullptr};
         return &o;
     }
 };

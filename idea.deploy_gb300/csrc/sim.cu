@@ -212,6 +212,8 @@ struct sclbm_sim {
     double *red = nullptr;
     int red_blocks = 0;
     int dgrid = 0, fgrid = 0, ugrid = 0;
+    FusedGeom fg = {};
+    int fused_grid = 0, path = SCLBM_PATH_AUTO, chunk_override = 0;
     bool n_set = false, u_set = false, pop_set = false, moments_fresh = false;
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int64_t device_bytes = 0;
@@ -291,13 +293,59 @@ int stencil_order(int D, const int *e, int qe) {
     return 0;
 }
 
-int launch_step(sclbm_sim *s) {
+bool fused_path(const sclbm_sim *s) { return s->ops->fused != nullptr && s->path != SCLBM_PATH_TWO_PASS; }
+
+// enqueue the kernels of one step; ev (optional) gets an event after each kernel
+int launch_step(sclbm_sim *s, cudaEvent_t *ev = nullptr) {
     const KernelOps *o = s->ops;
-    cudaError_t e = o->density(s->pop[s->cur], s->dn, s->psi, s->sp.data(), s->dgrid, s->st);
-    if (e == cudaSuccess) e = o->fcs(s->pop[s->cur], s->pop[s->cur ^ 1], s->dn, s->psi, s->sp.data(), s->fgrid, s->st);
+    cudaError_t e;
+    if (fused_path(s)) {
+        e = o->fused(s->pop[s->cur], s->pop[s->cur ^ 1], s->sp.data(), s->fg, s->fused_grid, s->st);
+        if (ev && e == cudaSuccess) e = cudaEventRecord(ev[0], s->st);
+    } else {
+        e = o->density(s->pop[s->cur], s->dn, s->psi, s->sp.data(), s->dgrid, s->st);
+        if (ev && e == cudaSuccess) e = cudaEventRecord(ev[0], s->st);
+        if (e == cudaSuccess)
+            e = o->fcs(s->pop[s->cur], s->pop[s->cur ^ 1], s->dn, s->psi, s->sp.data(), s->fgrid, s->st);
+        if (ev && e == cudaSuccess) e = cudaEventRecord(ev[1], s->st);
+    }
     if (e != cudaSuccess) return fail(SCLBM_ERR_CUDA, "step launch: %s", cudaGetErrorString(e));
     s->cur ^= 1;
     return SCLBM_OK;
+}
+
+// work decomposition of the single-pass kernel: tiles of the leading
+// dimensions x chunks of the marching dimension, sized so the items fill the
+// resident CTAs in whole waves with a small halo-plane overhead per chunk
+void plan_fused(sclbm_sim *s) {
+    const KernelOps *o = s->ops;
+    if (!o->fused) return;
+    FusedGeom &g = s->fg;
+    for (int d = 0; d < 3; d++) g.L[d] = d < s->D ? s->L[d] : 1;
+    g.V = s->V;
+    g.tiles_x = (s->L[0] + o->fused_tx - 1) / o->fused_tx;
+    g.tiles_y = s->D == 3 ? (s->L[1] + o->fused_ty - 1) / o->fused_ty : 1;
+    const int Lm = s->D == 3 ? s->L[2] : s->L[1];
+    const int resident = s->sms * o->fused_occupancy();
+    const int base = g.tiles_x * g.tiles_y;
+    int best_c = 1;
+    double best = -1;
+    for (int c = 1; c <= std::max(1, Lm / (2 * o->fused_r + 2)); c++) {
+        const int chunk = (Lm + c - 1) / c;
+        const int items = base * ((Lm + chunk - 1) / chunk);
+        const int waves = (items + resident - 1) / resident;
+        const double fill = (double)items / ((double)waves * resident);
+        const double halo = (double)chunk / (chunk + 2.0 * o->fused_r);
+        const double eff = std::min(1.0, fill * 1.25) * halo;  // a wave at 80% occupancy still streams HBM
+        if (eff > best + 1e-9) {
+            best = eff;
+            best_c = c;
+        }
+    }
+    g.chunk = s->chunk_override > 0 ? std::min(s->chunk_override, Lm) : (Lm + best_c - 1) / best_c;
+    g.chunks = (Lm + g.chunk - 1) / g.chunk;
+    g.items = base * g.chunks;
+    s->fused_grid = std::max(1, std::min(g.items, resident));
 }
 
 int build_graph(sclbm_sim *s, int parity) {
@@ -506,6 +554,7 @@ int configure(sclbm_sim *s, int collision, double tau, const double *mrt_s, cons
     const int64_t need_d = (s->V + 255) / 256, need_f = (s->V + 127) / 128;
     s->dgrid = (int)std::max<int64_t>(1, std::min<int64_t>(s->dgrid, need_d));
     s->fgrid = (int)std::max<int64_t>(1, std::min<int64_t>(s->fgrid, need_f));
+    plan_fused(s);
     return SCLBM_OK;
 }
 
@@ -652,7 +701,7 @@ int sclbm_info(const sclbm_sim *s, int64_t *volume, int64_t *device_bytes) {
 
 int sclbm_kernels_per_step(const sclbm_sim *s, int *count) {
     if (!s || !count) return fail(SCLBM_ERR_ARG, "null argument");
-    *count = s->ops->kernels_per_step;
+    *count = fused_path(s) ? 1 : 2;
     return SCLBM_OK;
 }
 
@@ -778,31 +827,56 @@ int sclbm_profile_step(sclbm_sim *s, int64_t nsteps, double *ms, int nms) {
     if (!s->pop_set) return fail(SCLBM_ERR_STATE, "populations are not initialized");
     if (nsteps < 1 || nsteps > 4096) return fail(SCLBM_ERR_ARG, "nsteps in [1, 4096]");
     DevGuard dg(s->device);
+    // per step: an event before the step, then one after each kernel
     std::vector<cudaEvent_t> ev((size_t)nsteps * 3);
     for (auto &e : ev) CUDA_TRY(cudaEventCreate(&e));
-    const KernelOps *o = s->ops;
-    for (int64_t i = 0; i < nsteps; i++) {
+    const bool fused = fused_path(s);
+    int rc = SCLBM_OK;
+    for (int64_t i = 0; i < nsteps && rc == SCLBM_OK; i++) {
         cudaEventRecord(ev[3 * i], s->st);
-        o->density(s->pop[s->cur], s->dn, s->psi, s->sp.data(), s->dgrid, s->st);
-        cudaEventRecord(ev[3 * i + 1], s->st);
-        o->fcs(s->pop[s->cur], s->pop[s->cur ^ 1], s->dn, s->psi, s->sp.data(), s->fgrid, s->st);
-        cudaEventRecord(ev[3 * i + 2], s->st);
-        s->cur ^= 1;
+        rc = launch_step(s, &ev[3 * i + 1]);
     }
     cudaError_t ce = cudaStreamSynchronize(s->st);
     double t0 = 0, t1 = 0;
-    for (int64_t i = 0; i < nsteps && ce == cudaSuccess; i++) {
+    for (int64_t i = 0; i < nsteps && ce == cudaSuccess && rc == SCLBM_OK; i++) {
         float a = 0, b = 0;
         cudaEventElapsedTime(&a, ev[3 * i], ev[3 * i + 1]);
-        cudaEventElapsedTime(&b, ev[3 * i + 1], ev[3 * i + 2]);
-        t0 += a;
-        t1 += b;
+        if (!fused) cudaEventElapsedTime(&b, ev[3 * i + 1], ev[3 * i + 2]);
+        if (fused) t1 += a;
+        else {
+            t0 += a;
+            t1 += b;
+        }
     }
     for (auto &e : ev) cudaEventDestroy(e);
     s->moments_fresh = false;
+    if (rc) return rc;
     if (ce != cudaSuccess) return fail(SCLBM_ERR_CUDA, "profile: %s", cudaGetErrorString(ce));
-    ms[0] = t0 / nsteps;
-    ms[1] = t1 / nsteps;
+    ms[0] = t0 / nsteps;  // density + psi pass (0 on the single-pass path)
+    ms[1] = t1 / nsteps;  // force + collide + stream (the whole step on the single-pass path)
+    return SCLBM_OK;
+}
+
+int sclbm_set_tuning(sclbm_sim *s, int path, int chunk) {
+    if (!s) return fail(SCLBM_ERR_ARG, "null handle");
+    if (path < SCLBM_PATH_AUTO || path > SCLBM_PATH_FUSED) return fail(SCLBM_ERR_ARG, "path %d", path);
+    if (path == SCLBM_PATH_FUSED && !s->ops->fused)
+        return fail(SCLBM_ERR_UNSUPPORTED, "single-pass kernel is built for FP32-shifted storage only");
+    DevGuard dg(s->device);
+    CUDA_TRY(cudaStreamSynchronize(s->st));
+    s->path = path;
+    s->chunk_override = chunk > 0 ? chunk : 0;
+    plan_fused(s);
+    for (auto &g : s->graph)
+        if (g) cudaGraphExecDestroy(g), g = nullptr;
+    return SCLBM_OK;
+}
+
+int sclbm_get_tuning(const sclbm_sim *s, int *path, int *chunk, int *grid) {
+    if (!s) return fail(SCLBM_ERR_ARG, "null handle");
+    if (path) *path = fused_path(s) ? SCLBM_PATH_FUSED : SCLBM_PATH_TWO_PASS;
+    if (chunk) *chunk = fused_path(s) ? s->fg.chunk : 0;
+    if (grid) *grid = fused_path(s) ? s->fused_grid : s->fgrid;
     return SCLBM_OK;
 }
 

@@ -13,6 +13,7 @@ from . import build as _build
 
 OK, ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA, ERR_STATE, ERR_NOMEM, ERR_NODEVICE = range(7)
 PSI_EXP_INV, PSI_ONE_MINUS_EXP, PSI_IDENTITY = 0, 1, 2
+PATH_AUTO, PATH_TWO_PASS, PATH_FUSED = 0, 1, 2
 COLL_BGK, COLL_MRT = 0, 1
 FP64, FP32_SHIFTED = 0, 1
 LIT_ROUND15, LIT_EXACT = 0, 1
@@ -72,6 +73,8 @@ SIGNATURES = {
     'sclbm_step_timed': [_P, _I64, _DP],
     'sclbm_profile_step': [_P, _I64, _DP, ctypes.c_int],
     'sclbm_kernels_per_step': [_P, _IP],
+    'sclbm_set_tuning': [_P, ctypes.c_int, ctypes.c_int],
+    'sclbm_get_tuning': [_P, _IP, _IP, _IP],
     'sclbm_compute_moments': [_P],
     'sclbm_reductions': [_P, _DP, _DP],
     'sclbm_check_u': [_P, _DP, _DP],
@@ -247,6 +250,14 @@ class Sim:
         c = ctypes.c_int()
         call('sclbm_kernels_per_step', self.h, ctypes.byref(c))
         return c.value
+
+    def set_tuning(self, path=0, chunk=0):
+        call('sclbm_set_tuning', self.h, int(path), int(chunk))
+
+    def get_tuning(self):
+        p, c, g = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        call('sclbm_get_tuning', self.h, ctypes.byref(p), ctypes.byref(c), ctypes.byref(g))
+        return p.value, c.value, g.value
 
     def info(self):
         v, b = ctypes.c_int64(), ctypes.c_int64()

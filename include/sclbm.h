@@ -163,6 +163,14 @@ SCLBM_API int sclbm_profile_step(sclbm_sim *s, int64_t nsteps, double *ms, int n
 /* count of kernels launched by sclbm_step per lattice step */
 SCLBM_API int sclbm_kernels_per_step(const sclbm_sim *s, int *count);
 
+/* step path: AUTO = single pass where built (FP32-shifted), else two passes */
+#define SCLBM_PATH_AUTO     0
+#define SCLBM_PATH_TWO_PASS 1  /* density+psi pass, then force+collide+stream pass */
+#define SCLBM_PATH_FUSED    2  /* one pass, psi recomputed in a shared-memory halo ring */
+/* choose the step path and the marching chunk (planes per work item, 0 = planned) */
+SCLBM_API int sclbm_set_tuning(sclbm_sim *s, int path, int chunk);
+SCLBM_API int sclbm_get_tuning(const sclbm_sim *s, int *path, int *chunk, int *grid);
+
 /* observables */
 SCLBM_API int sclbm_compute_moments(sclbm_sim *s);
 /* sum of all populations (FP64 accumulation) and total momentum sum_q xi_q f_q */
