@@ -305,6 +305,7 @@ def run_ours(a, dist):
     finite, nmax = sim.density_finite()
     # per-kernel device time of the dominant kernel (events on the handle's stream)
     k_ms = sim.profile_step(20)
+    path, chunk, grid = sim.get_tuning()
     sim.close()
     total = dist.ws * V * a.steps
     mlups = total / (ms / 1e3) / 1e6
@@ -321,7 +322,11 @@ def run_ours(a, dist):
                    'collision': 'MRT (rates 1.0)', 'precision': 'FP32 deviations from w_q*rho0, FP64 reductions',
                    'l2': 'inputs larger than L2 (populations 2 x %.2f GB)' % (Q * 4 * V / 1e9),
                    'parallelism': 'replicas x%d' % dist.ws if dist.ws > 1 else 'single GPU'},
-        'roofline': {'bound': 'hbm', 'kernel': 'k_fcs (force+collide+push-stream pass)',
+        'step_path': {'path': 'single pass (k_fused)' if path == 2 else 'two passes (k_density_psi + k_fcs)',
+                      'chunk_planes': chunk, 'grid': grid,
+                      'collision_kernel': 'MRT with all rates 1.0 is exactly BGK with omega=1: sparse BGK operator'},
+        'roofline': {'bound': 'hbm', 'kernel': 'k_fused (single pass)' if path == 2 else
+                     'k_fcs (force+collide+push-stream pass)',
                      'achieved': round(ach, 1), 'peak': hbm, 'unit': 'GB/s', 'frac': round(ach / hbm, 4),
                      'peak_source': 'MEASURED_PEAKS.json hbm_gbs (measured copy)' if pk else 'fallback 6.8 TB/s',
                      'traffic': None, 'alg_bytes_per_launch': alg_bytes,
@@ -333,6 +338,22 @@ def run_ours(a, dist):
         'finite_density_at_end': finite, 'max_density_at_end': nmax,
     }
     if dist.rank == 0 and dist.ws == 1:
+        # the general (dense-operator) MRT kernel, non-uniform rates, same box
+        rates = np.array([1.0] * 4 + [1.2] * 6 + [1.4] * 9)
+        from sclbm import _lib, XIStencils, FStencils
+        x, f = XIStencils['D3Q19'], FStencils['D3E6']
+        sg = _lib.Sim(3, BOX, x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], G, collision=_lib.COLL_MRT,
+                      mrt_s=np.diag(rates), precision=_lib.FP32_SHIFTED, rho0=0.5 * (RHO_L + RHO_G), device=dev)
+        sg.set_density(n0)
+        sg.set_velocity(np.zeros(3 * V))
+        sg.init_populations()
+        sg.step(2)
+        kg = max(10, a.steps // 10)
+        msg = sg.step_timed(kg)
+        sg.close()
+        out['mrt_general'] = {'value': round(V * kg / (msg / 1e3) / 1e6, 1), 'unit': 'MLUPS', 'steps': kg,
+                              'rates': 'rho,j: 1.0; stress: 1.2; higher moments: 1.4',
+                              'note': 'dense population-space MRT operator (Q x Q + Q x K per cell)'}
         # plain FP64 path on the same workload (secondary)
         s64 = make_sim('fp64', dev)
         s64.set_density(n0)

@@ -367,7 +367,7 @@ int build_collision(const CollisionSpec &s, CollisionTables &t, std::string &err
             for (int k = 0; k < K; k++) t.Beq[(size_t)q * K + k] = lit(m[k]);
         }
         if (s.collision == 0) {
-            Rat om = from_double(1.0 / s.tau);
+            Rat om = from_double(s.omega > 0 ? s.omega : 1.0 / s.tau);
             Rat g = Rat(1) - om / Rat(2);
             for (int q = 0; q < Q; q++) {
                 std::vector<Rat> m;

@@ -13,6 +13,7 @@ struct CollisionSpec {
     double c2 = 0;
     int collision = 0;            // 0 BGK, 1 MRT
     double tau = 1;
+    double omega = 0;             // BGK rate; > 0 overrides 1/tau
     const double *mrt_s = nullptr;  // q*q relaxation matrix (moment basis)
     int literals = 0;             // 0 round to 15 digits, 1 exact
 };

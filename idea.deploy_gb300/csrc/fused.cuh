@@ -104,12 +104,13 @@ __global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
                 for (int a = 0; a < S::QE; a++) {
                     const int em = D == 3 ? S::e(a, 2) : S::e(a, 1);
                     const int ey = D == 3 ? S::e(a, 1) : 0;
-                    const float ps = ring[wrapm(m + em, RING) * HC + (ty + R + ey) * HX + (tx + R + S::e(a, 0))];
+                    const int row = D == 3 ? (ty + R + ey) : 0;  // 2D: one halo row per plane
+                    const float ps = ring[wrapm(m + em, RING) * HC + row * HX + (tx + R + S::e(a, 0))];
 #pragma unroll
                     for (int c = 0; c < D; c++)
                         if (S::e(a, c) != 0) F[c] = fmaf(p.sw[a][c], ps, F[c]);
                 }
-                const float ps0 = ring[wrapm(m, RING) * HC + (ty + R) * HX + (tx + R)];
+                const float ps0 = ring[wrapm(m, RING) * HC + (D == 3 ? (ty + R) * HX : 0) + (tx + R)];
                 const float sc = p.neg_g * ps0;
 #pragma unroll
                 for (int c = 0; c < D; c++) F[c] *= sc;

@@ -506,6 +506,21 @@ int configure(sclbm_sim *s, int collision, double tau, const double *mrt_s, cons
     if (collision == SCLBM_COLL_BGK && !coll_a && !(tau > 0)) return fail(SCLBM_ERR_ARG, "tau must be > 0");
     if (collision == SCLBM_COLL_MRT && !coll_a && !mrt_s)
         return fail(SCLBM_ERR_ARG, "MRT needs the relaxation matrix mrt_s");
+    // MRT whose relaxation matrix is s*I is exactly BGK with omega = s (the
+    // equilibrium part M^-1 S M, the relaxation M^-1 (I-S) M and the Guo part
+    // Mn^-1 (I - S/2) Mn all reduce to multiples of I): the fused-arithmetic
+    // paths run the sparse BGK kernels for it; the reference-arithmetic path
+    // keeps the reference's expanded MRT expression.
+    double uniform_rate = 0;
+    if (collision == SCLBM_COLL_MRT && !coll_a && mrt_s && !(!s->fp32 && s->literals == SCLBM_LIT_ROUND15)) {
+        bool uni = mrt_s[0] > 0;
+        for (int i = 0; i < s->Q && uni; i++)
+            for (int j = 0; j < s->Q && uni; j++) uni = mrt_s[(size_t)i * s->Q + j] == (i == j ? mrt_s[0] : 0.0);
+        if (uni) {
+            uniform_rate = mrt_s[0];
+            collision = SCLBM_COLL_BGK;
+        }
+    }
     CollisionSpec cs;
     cs.dim = s->D;
     cs.q = s->Q;
@@ -514,6 +529,7 @@ int configure(sclbm_sim *s, int collision, double tau, const double *mrt_s, cons
     cs.c2 = s->c2;
     cs.collision = coll_a ? SCLBM_COLL_BGK : collision;  // equilibrium table always built
     cs.tau = coll_a ? 1.0 : tau;
+    cs.omega = coll_a ? 0.0 : uniform_rate;
     cs.mrt_s = mrt_s;
     cs.literals = s->fp32 ? SCLBM_LIT_EXACT : s->literals;
     CollisionTables t;
