@@ -11,6 +11,12 @@
 // Storage: FP32 deviations g_q = f_q - w_q rho0.  The rest population is set
 // from mass conservation, g*_0 = dn - sum_{q>0} g*_q, so FP32 rounding of the
 // collision coefficients cannot drift the total mass.
+//
+// Index arithmetic is kept off the critical path: cell offsets are 32-bit
+// (V < 2^31, checked on the host), the halo cells a thread reduces and the
+// wrapped neighbour rows / planes are computed once per tile or plane, and
+// every shared-memory stencil read has a compile-time offset from one of the
+// 2R+1 per-plane slot bases.
 #pragma once
 
 #include "kernels.cuh"
@@ -27,6 +33,7 @@ struct FusedShape {
     static constexpr int HX = TX + 2 * R;            // halo tile width
     static constexpr int HY = D == 3 ? TY + 2 * R : 1;
     static constexpr int HC = HX * HY;               // halo cells per plane
+    static constexpr int HPT = (HC + NT - 1) / NT;   // halo cells per thread
     static constexpr int RING = 2 * R + 1;           // psi planes kept
     static constexpr int SMEM = RING * HC * 4;       // bytes of the psi ring
 };
@@ -43,6 +50,28 @@ __device__ __forceinline__ int wrapm(int x, int L) {
     return r < 0 ? r + L : r;
 }
 
+// BGK + Guo collision of one cell in FP32-shifted variables (c2 = 1/3), factored:
+//   g*_q = (1-w) g_q + w_q [ C0 + eu (a eu + b + c eF) + d eF ]
+// eu = xi_q.u, eF = xi_q.F, C0 = w dn - 1.5 w n u^2 - 3 (1-w/2) u.F,
+// a = 4.5 w n, b = 3 w n, c = 9 (1-w/2), d = 3 (1-w/2); the same operator as
+// the expanded form (2nd-order Hermite equilibrium + Guo term, Collisions.py:163-185).
+template <class L, class S>
+__device__ __forceinline__ float bgk_fp32(const float *f, const float *u, const float *F, int q,
+                                          const StepParams<L, S, float> &p, float C0, float a, float b) {
+    constexpr int D = L::D;
+    float eu = 0.f, eF = 0.f;
+#pragma unroll
+    for (int c = 0; c < D; c++) {
+        if (L::xi(q, c) > 0) { eu += u[c]; eF += F[c]; }
+        if (L::xi(q, c) < 0) { eu -= u[c]; eF -= F[c]; }
+    }
+    float t = fmaf(a, eu, b);
+    t = fmaf(p.fc, eF, t);
+    t = fmaf(eu, t, p.fd * eF);
+    const float rhs = p.wq[q] * (C0 + t);
+    return p.a_nonzero ? fmaf(p.A[q][q], f[q], rhs) : rhs;
+}
+
 template <class L, class S, bool MRT>
 __global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
     k_fused(const float *__restrict__ pop, float *__restrict__ pop_out, const __grid_constant__ StepParams<L, S, float> p,
@@ -51,9 +80,10 @@ __global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
     constexpr int D = L::D, Q = L::Q, R = SH::R, HX = SH::HX, HC = SH::HC, NT = SH::NT, RING = SH::RING;
     extern __shared__ float ring[];  // [RING][HC]
     const int tid = threadIdx.x;
-    const int64_t V = fg.V;
+    const int V = (int)fg.V;
     const int Lx = fg.L[0], Ly = fg.L[1], Lz = fg.L[2];
-    const int Lm = D == 3 ? Lz : Ly;  // marching extent
+    const int Lm = D == 3 ? Lz : Ly;                 // marching extent
+    const int PL = D == 3 ? Lx * Ly : Lx;            // cells per plane
     const int tx = tid % SH::TX, ty = D == 3 ? tid / SH::TX : 0;
 
     for (int item = blockIdx.x; item < fg.items; item += gridDim.x) {
@@ -64,20 +94,39 @@ __global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
         const int x0 = ix * SH::TX, y0 = iy * SH::TY;
         const int m0 = ic * fg.chunk, m1 = min(m0 + fg.chunk, Lm);
 
-        // n and psi of the halo tile of plane m into its ring slot
+        // in-plane offsets of the halo cells this thread reduces (fixed per tile)
+        int hoff[SH::HPT];
+#pragma unroll
+        for (int k = 0; k < SH::HPT; k++) {
+            const int c = tid + k * NT;
+            const int hx = c % HX, hy = c / HX;
+            const int gx = wrapm(x0 - R + hx, Lx);
+            hoff[k] = D == 3 ? gx + Lx * wrapm(y0 - R + hy, Ly) : gx;
+        }
+        // interior cell of this thread and its wrapped neighbour columns / rows
+        const int x = x0 + tx, y = D == 3 ? y0 + ty : 0;
+        const bool in_tile = x < Lx && (D == 2 || y < Ly);
+        int X3[3], Y3[3];
+#pragma unroll
+        for (int o = -1; o <= 1; o++) {
+            X3[o + 1] = wrapc(x + o, Lx);
+            Y3[o + 1] = D == 3 ? Lx * wrapc(y + o, Ly) : 0;
+        }
+        const int own = X3[1] + Y3[1];
+
         auto psi_plane = [&](int m) {
             float *slot = ring + wrapm(m, RING) * HC;
-            const int gm = wrapm(m, Lm);
-            for (int c = tid; c < HC; c += NT) {
-                const int hx = c % HX, hy = c / HX;
-                const int gx = wrapm(x0 - R + hx, Lx);
-                int64_t g;
-                if (D == 3) g = gx + (int64_t)Lx * (wrapm(y0 - R + hy, Ly) + (int64_t)Ly * gm);
-                else g = gx + (int64_t)Lx * gm;
-                float s = __ldg(pop + (int64_t)lex_q<Q>(0) * V + g);
+            const int poff = wrapm(m, Lm) * PL;
 #pragma unroll
-                for (int i = 1; i < Q; i++) s += __ldg(pop + (int64_t)lex_q<Q>(i) * V + g);
-                slot[c] = psi_of<float>(p.psi_kind, p.rho0 + s);
+            for (int k = 0; k < SH::HPT; k++) {
+                const int c = tid + k * NT;
+                if (k + 1 < SH::HPT || c < HC) {
+                    const float *src = pop + (poff + hoff[k]);
+                    float s = __ldg(src + lex_q<Q>(0) * V);
+#pragma unroll
+                    for (int i = 1; i < Q; i++) s += __ldg(src + lex_q<Q>(i) * V);
+                    slot[c] = psi_of<float>(p.psi_kind, p.rho0 + s);
+                }
             }
         };
 
@@ -85,61 +134,60 @@ __global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
         for (int m = m0; m < m1; m++) {
             psi_plane(m + R);
             __syncthreads();
-            const int x = x0 + tx, y = D == 3 ? y0 + ty : m;
-            const bool inside = x < Lx && (D == 2 || y < Ly);
-            if (inside) {
-                const int z = D == 3 ? m : 0;
-                const int64_t g = D == 3 ? x + (int64_t)Lx * (y + (int64_t)Ly * z) : x + (int64_t)Lx * y;
+            if (in_tile) {
+                // slot bases of planes m-R .. m+R, offset to this thread's halo position
+                const float *sb[RING];
+#pragma unroll
+                for (int k = 0; k < RING; k++) sb[k] = ring + wrapm(m + k - R, RING) * HC + ty * HX + tx;
+                int Z3[3];
+#pragma unroll
+                for (int o = -1; o <= 1; o++) Z3[o + 1] = D == 3 ? wrapc(m + o, Lm) * PL : wrapc(m + o, Lm) * Lx;
+                const int g = own + Z3[1];
                 float f[Q];
 #pragma unroll
-                for (int q = 0; q < Q; q++) f[q] = __ldg(pop + (int64_t)q * V + g);
+                for (int q = 0; q < Q; q++) f[q] = __ldg(pop + (g + q * V));
                 float d = f[lex_q<Q>(0)];
 #pragma unroll
                 for (int i = 1; i < Q; i++) d += f[lex_q<Q>(i)];
-                // Shan-Chen force from the psi ring
+                // Shan-Chen force from the psi ring (compile-time offsets)
                 float F[D];
 #pragma unroll
-                for (int a = 0; a < D; a++) F[a] = 0.f;
+                for (int c = 0; c < D; c++) F[c] = 0.f;
 #pragma unroll
                 for (int a = 0; a < S::QE; a++) {
                     const int em = D == 3 ? S::e(a, 2) : S::e(a, 1);
                     const int ey = D == 3 ? S::e(a, 1) : 0;
-                    const int row = D == 3 ? (ty + R + ey) : 0;  // 2D: one halo row per plane
-                    const float ps = ring[wrapm(m + em, RING) * HC + row * HX + (tx + R + S::e(a, 0))];
+                    const float ps = sb[em + R][(D == 3 ? (R + ey) * HX : 0) + R + S::e(a, 0)];
 #pragma unroll
                     for (int c = 0; c < D; c++)
                         if (S::e(a, c) != 0) F[c] = fmaf(p.sw[a][c], ps, F[c]);
                 }
-                const float ps0 = ring[wrapm(m, RING) * HC + (D == 3 ? (ty + R) * HX : 0) + (tx + R)];
-                const float sc = p.neg_g * ps0;
+                const float sc = p.neg_g * sb[R][(D == 3 ? R * HX : 0) + R];
 #pragma unroll
                 for (int c = 0; c < D; c++) F[c] *= sc;
                 const float n = p.rho0 + d;
                 float u[D];
                 velocity<L, float>(f, n, F, u);
-                float out[Q];
-                float rest = d;
+                // collision + push stream; rest population last, from mass conservation
+                float u2 = 0.f, uF = 0.f;
+#pragma unroll
+                for (int c = 0; c < D; c++) {
+                    u2 = fmaf(u[c], u[c], u2);
+                    uF = fmaf(u[c], F[c], uF);
+                }
+                const float C0 = p.omega * d - p.om15 * n * u2 - p.fd * uF;
+                const float a = p.om45 * n, b = p.om3 * n;
+                float rest_pop = d;
 #pragma unroll
                 for (int q = 1; q < Q; q++) {
-                    collide_cell<L, S, MRT, float, false>(f, d, n, u, F, q, p, out[q]);
-                    rest -= out[q];
+                    float out;
+                    if (MRT) collide_cell<L, S, true, float, false>(f, d, n, u, F, q, p, out);
+                    else out = bgk_fp32<L, S>(f, u, F, q, p, C0, a, b);
+                    rest_pop -= out;
+                    const int dst = X3[L::xi(q, 0) + 1] + Y3[L::xi(q, 1) + 1] + Z3[L::xi(q, D - 1) + 1];
+                    pop_out[dst + q * V] = out;
                 }
-                out[0] = rest;
-                // push stream
-                int xs[3], ys[3], zs[3];
-#pragma unroll
-                for (int o = -1; o <= 1; o++) {
-                    xs[o + 1] = wrapc(x + o, Lx);
-                    ys[o + 1] = wrapc(y + o, Ly);
-                    zs[o + 1] = D == 3 ? wrapc(z + o, Lz) : 0;
-                }
-#pragma unroll
-                for (int q = 0; q < Q; q++) {
-                    const int X = xs[L::xi(q, 0) + 1], Y = ys[L::xi(q, 1) + 1];
-                    int64_t dst = X + (int64_t)Lx * Y;
-                    if (D == 3) dst += (int64_t)Lx * Ly * zs[L::xi(q, 2) + 1];
-                    pop_out[(int64_t)q * V + dst] = out[q];
-                }
+                pop_out[g] = rest_pop;
             }
             __syncthreads();
         }

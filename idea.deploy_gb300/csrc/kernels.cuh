@@ -36,6 +36,10 @@ struct StepParams {
     Real sw[QE][D]; // signed force weights e_{a,d} * w_a
     Real A[Q][Q];   // population operator (BGK: diagonal used)
     Real B[Q][K];   // monomial coefficients
+    // factored BGK (single-pass FP32 kernel): omega, 1.5 omega, 3 omega,
+    // 4.5 omega, 9 (1 - omega/2), 3 (1 - omega/2), lattice weights
+    Real omega, om15, om3, om45, fc, fd;
+    Real wq[Q];
 };
 
 template <class L, class Real>

@@ -26,6 +26,8 @@ struct HostSetup {
     const double *B;    // q*K
     const double *Beq;  // q*K
     bool a_nonzero;
+    double omega;       // BGK rate (factored single-pass collision), 0 if not BGK
+    const double *w;    // q lattice weights
 };
 
 struct KernelOps {
@@ -75,6 +77,14 @@ struct Ops {
             for (int j = 0; j < Q; j++) p->A[i][j] = (Real)h.A[i * Q + j];
         for (int i = 0; i < Q; i++)
             for (int k = 0; k < K; k++) p->B[i][k] = (Real)h.B[i * K + k];
+        const double w = h.omega;
+        p->omega = (Real)w;
+        p->om15 = (Real)(1.5 * w);
+        p->om3 = (Real)(3.0 * w);
+        p->om45 = (Real)(4.5 * w);
+        p->fc = (Real)(9.0 * (1.0 - 0.5 * w));
+        p->fd = (Real)(3.0 * (1.0 - 0.5 * w));
+        for (int i = 0; i < Q; i++) p->wq[i] = (Real)(h.w ? h.w[i] : 0.0);
     }
     static void fill_eq(void *params, const HostSetup &h) {
         EP *p = static_cast<EP *>(params);

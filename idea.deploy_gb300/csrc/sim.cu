@@ -293,7 +293,12 @@ int stencil_order(int D, const int *e, int qe) {
     return 0;
 }
 
-bool fused_path(const sclbm_sim *s) { return s->ops->fused != nullptr && s->path != SCLBM_PATH_TWO_PASS; }
+// the single-pass kernel indexes populations with 32-bit offsets (q*V + cell)
+bool fused_fits(const sclbm_sim *s) { return (int64_t)s->Q * s->V < ((int64_t)1 << 31); }
+
+bool fused_path(const sclbm_sim *s) {
+    return s->ops->fused != nullptr && s->path != SCLBM_PATH_TWO_PASS && fused_fits(s);
+}
 
 // enqueue the kernels of one step; ev (optional) gets an event after each kernel
 int launch_step(sclbm_sim *s, cudaEvent_t *ev = nullptr) {
@@ -557,6 +562,8 @@ int configure(sclbm_sim *s, int collision, double tau, const double *mrt_s, cons
     h.B = t.B.data();
     h.Beq = t.Beq.data();
     h.a_nonzero = a_nonzero;
+    h.omega = (!mrt && !coll_a) ? (uniform_rate > 0 ? uniform_rate : 1.0 / tau) : 0.0;
+    h.w = s->w.data();
     for (auto &g : s->graph)
         if (g) cudaGraphExecDestroy(g), g = nullptr;
     s->K = t.K;
@@ -878,6 +885,8 @@ int sclbm_set_tuning(sclbm_sim *s, int path, int chunk) {
     if (path < SCLBM_PATH_AUTO || path > SCLBM_PATH_FUSED) return fail(SCLBM_ERR_ARG, "path %d", path);
     if (path == SCLBM_PATH_FUSED && !s->ops->fused)
         return fail(SCLBM_ERR_UNSUPPORTED, "single-pass kernel is built for FP32-shifted storage only");
+    if (path == SCLBM_PATH_FUSED && !fused_fits(s))
+        return fail(SCLBM_ERR_UNSUPPORTED, "single-pass kernel needs q*volume < 2^31");
     DevGuard dg(s->device);
     CUDA_TRY(cudaStreamSynchronize(s->st));
     s->path = path;
