@@ -34,9 +34,22 @@ struct FusedShape {
     static constexpr int HY = D == 3 ? TY + 2 * R : 1;
     static constexpr int HC = HX * HY;               // halo cells per plane
     static constexpr int HPT = (HC + NT - 1) / NT;   // halo cells per thread
-    static constexpr int RING = 2 * R + 1;           // psi planes kept
-    static constexpr int SMEM = RING * HC * 4;       // bytes of the psi ring
+    // psi planes kept: 2R+1 in use plus one being written, so one barrier per
+    // plane suffices (the slot written for plane m+R held plane m-R-2)
+    static constexpr int RING = 2 * R + 2;
+    static constexpr int STAGE = HPT * L::Q * NT;    // floats of one plane's staged halo populations
+    static constexpr int SMEM = (RING * HC + 2 * STAGE) * 4;  // psi ring + double-buffered stage
 };
+
+__device__ __forceinline__ void cp_async4(float *smem, const float *gmem) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(s), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
+}
 
 struct FusedGeom {
     int L[3];
@@ -78,7 +91,9 @@ __global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
             const FusedGeom fg) {
     using SH = FusedShape<L, S>;
     constexpr int D = L::D, Q = L::Q, R = SH::R, HX = SH::HX, HC = SH::HC, NT = SH::NT, RING = SH::RING;
-    extern __shared__ float ring[];  // [RING][HC]
+    extern __shared__ float smem[];  // psi ring [RING][HC], then 2 stage buffers [HPT][Q][NT]
+    float *ring = smem;
+    float *stage0 = smem + RING * HC;
     const int tid = threadIdx.x;
     const int V = (int)fg.V;
     const int Lx = fg.L[0], Ly = fg.L[1], Lz = fg.L[2];
@@ -114,6 +129,7 @@ __global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
         }
         const int own = X3[1] + Y3[1];
 
+        // n and psi of plane m straight from global memory (chunk preamble)
         auto psi_plane = [&](int m) {
             float *slot = ring + wrapm(m, RING) * HC;
             const int poff = wrapm(m, Lm) * PL;
@@ -129,10 +145,49 @@ __global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
                 }
             }
         };
+        // asynchronous copy of this thread's halo populations of plane m into a stage buffer
+        auto stage_issue = [&](int m) {
+            float *st = stage0 + (m & 1) * SH::STAGE;
+            const int poff = wrapm(m, Lm) * PL;
+#pragma unroll
+            for (int k = 0; k < SH::HPT; k++) {
+                const int c = tid + k * NT;
+                if (k + 1 < SH::HPT || c < HC) {
+                    const float *src = pop + (poff + hoff[k]);
+#pragma unroll
+                    for (int q = 0; q < Q; q++) cp_async4(st + (k * Q + q) * NT + tid, src + q * V);
+                }
+            }
+            cp_async_commit();
+        };
+        // n and psi of plane m from the stage (each thread reads back only its own copies)
+        auto stage_reduce = [&](int m) {
+            const float *st = stage0 + (m & 1) * SH::STAGE;
+            float *slot = ring + wrapm(m, RING) * HC;
+#pragma unroll
+            for (int k = 0; k < SH::HPT; k++) {
+                const int c = tid + k * NT;
+                if (k + 1 < SH::HPT || c < HC) {
+                    float s = st[(k * Q + lex_q<Q>(0)) * NT + tid];
+#pragma unroll
+                    for (int i = 1; i < Q; i++) s += st[(k * Q + lex_q<Q>(i)) * NT + tid];
+                    slot[c] = psi_of<float>(p.psi_kind, p.rho0 + s);
+                }
+            }
+        };
 
+        __syncthreads();  // the previous item's readers are done with the ring
         for (int m = m0 - R; m < m0 + R; m++) psi_plane(m);
+        stage_issue(m0 + R);
         for (int m = m0; m < m1; m++) {
-            psi_plane(m + R);
+            // prefetch plane m+R+1 while plane m+R is reduced and plane m collided
+            if (m + 1 < m1) {
+                stage_issue(m + R + 1);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
+            stage_reduce(m + R);
             __syncthreads();
             if (in_tile) {
                 // slot bases of planes m-R .. m+R, offset to this thread's halo position
@@ -189,7 +244,6 @@ __global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
                 }
                 pop_out[g] = rest_pop;
             }
-            __syncthreads();
         }
     }
 }

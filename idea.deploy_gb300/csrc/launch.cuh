@@ -129,15 +129,30 @@ struct Ops {
                              cudaStream_t st) {
         if constexpr (std::is_same<Real, float>::value) {
             using SH = FusedShape<L, S>;
+            allow_smem();
             k_fused<L, S, MRT><<<grid, SH::NT, SH::SMEM, st>>>((const float *)pop, (float *)pop_out,
                                                                *static_cast<const SP *>(sp), fg);
             return cudaGetLastError();
         }
         return cudaErrorNotSupported;
     }
+    // the single-pass kernel's shared memory (psi ring + stage) exceeds the 48 KB default
+    static void allow_smem() {
+        if constexpr (std::is_same<Real, float>::value) {
+            static bool done[64] = {};  // per device
+            int dev = 0;
+            cudaGetDevice(&dev);
+            if (dev < 0 || dev >= 64 || !done[dev]) {
+                cudaFuncSetAttribute(k_fused<L, S, MRT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     FusedShape<L, S>::SMEM);
+                if (dev >= 0 && dev < 64) done[dev] = true;
+            }
+        }
+    }
     static int fused_occupancy() {
         if constexpr (std::is_same<Real, float>::value) {
             using SH = FusedShape<L, S>;
+            allow_smem();
             int b = 0;
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fused<L, S, MRT>, SH::NT, SH::SMEM);
             return b > 0 ? b : 1;
