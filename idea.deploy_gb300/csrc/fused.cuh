@@ -37,7 +37,8 @@ struct FusedShape {
     // psi planes kept: 2R+1 in use plus one being written, so one barrier per
     // plane suffices (the slot written for plane m+R held plane m-R-2)
     static constexpr int RING = 2 * R + 2;
-    static constexpr int STAGE = HPT * L::Q * NT;    // floats of one plane's staged halo populations
+    // floats of one plane's staged halo populations (2D only: see k_fused)
+    static constexpr int STAGE = D == 2 ? HPT * L::Q * NT : 0;
     static constexpr int SMEM = (RING * HC + 2 * STAGE) * 4;  // psi ring + double-buffered stage
 };
 
@@ -176,31 +177,41 @@ __global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
             }
         };
 
+        // 2D: the halo of plane m+R+1 is prefetched with cp.async during plane m;
+        // 3D: the halo (1.7x the tile) is reduced straight from L2 and the
+        // thread's own populations of plane m are loaded first, so both sets of
+        // loads are in flight together
+        constexpr bool STAGED = D == 2;
         __syncthreads();  // the previous item's readers are done with the ring
         for (int m = m0 - R; m < m0 + R; m++) psi_plane(m);
-        stage_issue(m0 + R);
+        if (STAGED) stage_issue(m0 + R);
         for (int m = m0; m < m1; m++) {
-            // prefetch plane m+R+1 while plane m+R is reduced and plane m collided
-            if (m + 1 < m1) {
-                stage_issue(m + R + 1);
-                cp_async_wait<1>();
-            } else {
-                cp_async_wait<0>();
+            int Z3[3];
+#pragma unroll
+            for (int o = -1; o <= 1; o++) Z3[o + 1] = D == 3 ? wrapc(m + o, Lm) * PL : wrapc(m + o, Lm) * Lx;
+            const int g = own + Z3[1];
+            float f[Q];
+            if (in_tile) {
+#pragma unroll
+                for (int q = 0; q < Q; q++) f[q] = __ldg(pop + (g + q * V));
             }
-            stage_reduce(m + R);
+            if (STAGED) {
+                if (m + 1 < m1) {
+                    stage_issue(m + R + 1);
+                    cp_async_wait<1>();
+                } else {
+                    cp_async_wait<0>();
+                }
+                stage_reduce(m + R);
+            } else {
+                psi_plane(m + R);
+            }
             __syncthreads();
             if (in_tile) {
                 // slot bases of planes m-R .. m+R, offset to this thread's halo position
                 const float *sb[RING];
 #pragma unroll
                 for (int k = 0; k < RING; k++) sb[k] = ring + wrapm(m + k - R, RING) * HC + ty * HX + tx;
-                int Z3[3];
-#pragma unroll
-                for (int o = -1; o <= 1; o++) Z3[o + 1] = D == 3 ? wrapc(m + o, Lm) * PL : wrapc(m + o, Lm) * Lx;
-                const int g = own + Z3[1];
-                float f[Q];
-#pragma unroll
-                for (int q = 0; q < Q; q++) f[q] = __ldg(pop + (g + q * V));
                 float d = f[lex_q<Q>(0)];
 #pragma unroll
                 for (int i = 1; i < Q; i++) d += f[lex_q<Q>(i)];
