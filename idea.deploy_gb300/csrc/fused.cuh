@@ -59,6 +59,14 @@ struct FusedGeom {
     int items;
 };
 
+// FP32 pseudopotential with the fast hardware exp2/reciprocal (relative error
+// ~1e-7, below the FP32 storage of the populations)
+__device__ __forceinline__ float psi_fast(int kind, float n) {
+    if (kind == PSI_EXP_INV) return __expf(-__fdividef(1.f, n));
+    if (kind == PSI_ONE_MINUS_EXP) return 1.f - __expf(-n);
+    return n;
+}
+
 __device__ __forceinline__ int wrapm(int x, int L) {
     int r = x % L;
     return r < 0 ? r + L : r;
@@ -130,20 +138,27 @@ __global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
         }
         const int own = X3[1] + Y3[1];
 
-        // n and psi of plane m straight from global memory (chunk preamble)
+        // n and psi of plane m straight from global memory; every load is issued
+        // before the first sum (threads without a second halo cell re-read their
+        // first one and skip the store), so HPT*Q loads are in flight at once
         auto psi_plane = [&](int m) {
             float *slot = ring + wrapm(m, RING) * HC;
             const int poff = wrapm(m, Lm) * PL;
+            float v[SH::HPT][Q];
 #pragma unroll
             for (int k = 0; k < SH::HPT; k++) {
                 const int c = tid + k * NT;
-                if (k + 1 < SH::HPT || c < HC) {
-                    const float *src = pop + (poff + hoff[k]);
-                    float s = __ldg(src + lex_q<Q>(0) * V);
+                const float *src = pop + (poff + (c < HC ? hoff[k] : hoff[0]));
 #pragma unroll
-                    for (int i = 1; i < Q; i++) s += __ldg(src + lex_q<Q>(i) * V);
-                    slot[c] = psi_of<float>(p.psi_kind, p.rho0 + s);
-                }
+                for (int q = 0; q < Q; q++) v[k][q] = __ldg(src + q * V);
+            }
+#pragma unroll
+            for (int k = 0; k < SH::HPT; k++) {
+                const int c = tid + k * NT;
+                float s = v[k][lex_q<Q>(0)];
+#pragma unroll
+                for (int i = 1; i < Q; i++) s += v[k][lex_q<Q>(i)];
+                if (k + 1 < SH::HPT || c < HC) slot[c] = psi_fast(p.psi_kind, p.rho0 + s);
             }
         };
         // asynchronous copy of this thread's halo populations of plane m into a stage buffer
@@ -172,7 +187,7 @@ __global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
                     float s = st[(k * Q + lex_q<Q>(0)) * NT + tid];
 #pragma unroll
                     for (int i = 1; i < Q; i++) s += st[(k * Q + lex_q<Q>(i)) * NT + tid];
-                    slot[c] = psi_of<float>(p.psi_kind, p.rho0 + s);
+                    slot[c] = psi_fast(p.psi_kind, p.rho0 + s);
                 }
             }
         };

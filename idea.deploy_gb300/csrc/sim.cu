@@ -341,7 +341,7 @@ void plan_fused(sclbm_sim *s) {
         const int waves = (items + resident - 1) / resident;
         const double fill = (double)items / ((double)waves * resident);
         const double halo = (double)chunk / (chunk + 2.0 * o->fused_r);
-        const double eff = std::min(1.0, fill * 1.25) * halo;  // a wave at 80% occupancy still streams HBM
+        const double eff = fill * halo;  // resident-slot fill x share of planes that are not preamble
         if (eff > best + 1e-9) {
             best = eff;
             best_c = c;
