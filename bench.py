@@ -235,13 +235,25 @@ def peaks():
         return None
 
 
-def make_sim(precision, device):
+def make_sim(precision, device, literals='exact'):
     from sclbm import _lib, XIStencils, FStencils
     x, f = XIStencils['D3Q19'], FStencils['D3E6']
     S = np.eye(Q)
     return _lib.Sim(3, BOX, x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], G, collision=_lib.COLL_MRT, mrt_s=S,
                     precision=_lib.FP32_SHIFTED if precision == 'fp32' else _lib.FP64,
-                    rho0=0.5 * (RHO_L + RHO_G), device=device)
+                    rho0=0.5 * (RHO_L + RHO_G), device=device,
+                    literals=_lib.LIT_EXACT if literals == 'exact' else _lib.LIT_ROUND15)
+
+
+def profiled_traffic():
+    """DRAM bytes per launch of the single-pass kernel from the committed ncu
+    summary (captured on a smaller box and scaled by the cells it processes)."""
+    p = os.path.join(ROOT, 'profiles', 'k_fused_d3q19_e6_bgk_fp32.json')
+    try:
+        d = json.load(open(p))
+        return d['dram_bytes_per_cell'] * int(np.prod(BOX)), d
+    except Exception:
+        return None, None
 
 
 def e2e_measure(precision, device, iters=3, lbm_steps=200):
@@ -329,7 +341,8 @@ def run_ours(a, dist):
                      'k_fcs (force+collide+push-stream pass)',
                      'achieved': round(ach, 1), 'peak': hbm, 'unit': 'GB/s', 'frac': round(ach / hbm, 4),
                      'peak_source': 'MEASURED_PEAKS.json hbm_gbs (measured copy)' if pk else 'fallback 6.8 TB/s',
-                     'traffic': None, 'alg_bytes_per_launch': alg_bytes,
+                     'traffic': profiled_traffic()[0], 'alg_bytes_per_launch': alg_bytes,
+                     'traffic_source': (profiled_traffic()[1] or {}).get('source'),
                      'kernel_ms': round(k_ms[1], 4), 'density_pass_ms': round(k_ms[0], 4),
                      'step_alg_GBs': round(alg_bytes * a.steps / (ms / 1e3) / 1e9, 1),
                      'step_frac': round(alg_bytes * a.steps / (ms / 1e3) / 1e9 / hbm, 4)},
@@ -354,19 +367,24 @@ def run_ours(a, dist):
         out['mrt_general'] = {'value': round(V * kg / (msg / 1e3) / 1e6, 1), 'unit': 'MLUPS', 'steps': kg,
                               'rates': 'rho,j: 1.0; stress: 1.2; higher moments: 1.4',
                               'note': 'dense population-space MRT operator (Q x Q + Q x K per cell)'}
-        # plain FP64 path on the same workload (secondary)
-        s64 = make_sim('fp64', dev)
-        s64.set_density(n0)
-        s64.set_velocity(np.zeros(3 * V))
-        s64.init_populations()
-        s64.step(2)
-        k64 = max(4, a.steps // 50)
-        ms64 = s64.step_timed(k64)
-        kk = s64.profile_step(3)
-        s64.close()
-        out['fp64'] = {'value': round(V * k64 / (ms64 / 1e3) / 1e6, 1), 'unit': 'MLUPS', 'steps': k64,
-                       'ms_per_step': round(ms64 / k64, 4), 'kernel_ms': [round(kk[0], 4), round(kk[1], 4)],
-                       'alg_GBs': round(2 * Q * 8 * V * k64 / (ms64 / 1e3) / 1e9, 1)}
+        # plain FP64 path on the same workload (secondary): fused arithmetic with
+        # exact coefficients, and the reference's arithmetic (its literals and
+        # evaluation order, no FMA; GB300's FP64 rate bounds both)
+        out['fp64'] = {}
+        for lit, key in (('exact', 'fused_arithmetic'), ('round15', 'reference_arithmetic')):
+            s64 = make_sim('fp64', dev, literals=lit)
+            s64.set_density(n0)
+            s64.set_velocity(np.zeros(3 * V))
+            s64.init_populations()
+            s64.step(2)
+            k64 = max(4, a.steps // 100)
+            ms64 = s64.step_timed(k64)
+            kk = s64.profile_step(3)
+            s64.close()
+            out['fp64'][key] = {'value': round(V * k64 / (ms64 / 1e3) / 1e6, 1), 'unit': 'MLUPS', 'steps': k64,
+                                'ms_per_step': round(ms64 / k64, 4),
+                                'kernel_ms': [round(kk[0], 4), round(kk[1], 4)],
+                                'alg_GBs': round(2 * Q * 8 * V * k64 / (ms64 / 1e3) / 1e9, 1)}
         out['e2e'] = e2e_measure('fp32', dev)
         if not a.no_cpu:
             out['cpu_baseline'] = cpu_measure(a.cpu_seconds)
@@ -378,10 +396,22 @@ def run_reference(a, dist):
         return None
     threads = os.cpu_count() or 1
     got = _ref_kernels('d3q19_e6_mrt1_64')
-    runner = cpu_reference if got is not None else cpu_port
-    # bounded: calibrate one step, then size the per-step work to the K+W budget
-    mlups1, dt1, V, kind = runner(1, threads)
-    res = runner(a.warmup, threads) if a.warmup else None
+    # bounded: calibrate one step on the 64^3 sample box, then shrink the box
+    # (32^3, 16^3: the same generated kernels with the box-size constants
+    # re-set, as the reference sets them per box) until K+W steps fit ~150 s
+    tag = 'd3q19_e6_mrt1_64'
+    if got is not None:
+        runner = lambda n, t: cpu_reference(n, t, tag=tag)
+        dt1 = cpu_reference(1, threads, tag=tag)[1]
+        for smaller in ('d3q19_e6_mrt1_32', 'd3q19_e6_mrt1_16'):
+            if dt1 * (a.steps + a.warmup) <= 150.0 or _ref_kernels(smaller) is None:
+                break
+            tag = smaller
+            dt1 = cpu_reference(1, threads, tag=tag)[1]
+    else:
+        runner = cpu_port
+    if a.warmup:
+        runner(a.warmup, threads)
     mlups, dt, V, kind = runner(a.steps, threads)
     out = {'metric': METRIC, 'value': round(mlups, 3), 'unit': 'MLUPS', 'n_gpus': dist.ws, 'steps': a.steps,
            'warmup': a.warmup, 'ms_per_step': round(dt / a.steps * 1e3, 3), 'higher_is_better': True,
@@ -397,7 +427,7 @@ def run_reference(a, dist):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
-    ap.add_argument('--steps', type=int, default=1000)
+    ap.add_argument('--steps', type=int, default=2000)
     ap.add_argument('--warmup', type=int, default=5)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--cpu-seconds', type=float, default=15.0)

@@ -106,10 +106,43 @@ def generate(reference, only=None):
         print('generated', tag, flush=True)
 
 
+def box_variants():
+    """Smaller sample boxes of the 3D benchmark kernels (32^3, 16^3) for the
+    bounded CPU baseline: the generated sources take the box size only through
+    their #define constants (V, L_i, STR_i, N_THREADS), the values the
+    reference passes per box (idpy/IdpyCode/IdpyCode.py:567-611)."""
+    man = json.load(open(MANIFEST))
+    base = man.get('d3q19_e6_mrt1_64')
+    if base is None:
+        return
+    for L in (32, 16):
+        tag = 'd3q19_e6_mrt1_%d' % L
+        files = {}
+        for role, f in base['files'].items():
+            src = open(os.path.join(REF_DIR, f['file'])).read()
+            defs = {'V': L ** 3, 'L_0': L, 'L_1': L, 'L_2': L, 'STR_0': L, 'STR_1': L * L, 'N_THREADS': L ** 3}
+            lines = []
+            for line in src.split('\n'):
+                parts = line.split()
+                if len(parts) == 3 and parts[0] == '#define' and parts[1] in defs:
+                    line = '#define %s %d' % (parts[1], defs[parts[1]])
+                lines.append(line)
+            dst = '%s_%s.c' % (tag, role)
+            text = '\n'.join(lines)
+            path = os.path.join(REF_DIR, dst)
+            if not os.path.exists(path) or open(path).read() != text:
+                with open(path, 'w') as fh:
+                    fh.write(text)
+            files[role] = {'file': dst, 'kernel': f['kernel']}
+        man[tag] = dict(base, box=[L, L, L], files=files)
+    json.dump(man, open(MANIFEST, 'w'), indent=1)
+
+
 def build():
     """Compile the generated sources in oracle/_ref with the reference's flags."""
     if not os.path.exists(MANIFEST):
         return []
+    box_variants()
     out = []
     for src in sorted(glob.glob(os.path.join(REF_DIR, '*.c'))):
         so = src[:-2] + '.so'
