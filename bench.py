@@ -350,7 +350,7 @@ def run_ours(a, dist):
         'clocks': ck,
         'finite_density_at_end': finite, 'max_density_at_end': nmax,
     }
-    if dist.rank == 0 and dist.ws == 1:
+    if dist.rank == 0 and dist.ws == 1 and not a.main_only:
         # the general (dense-operator) MRT kernel, non-uniform rates, same box
         rates = np.array([1.0] * 4 + [1.2] * 6 + [1.4] * 9)
         from sclbm import _lib, XIStencils, FStencils
@@ -432,14 +432,18 @@ def main():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--cpu-seconds', type=float, default=15.0)
     ap.add_argument('--no-cpu', action='store_true')
+    # profiling case: a smaller cubic box and only the main (FP32 single-pass) leg
+    ap.add_argument('--box', type=int, default=0, help='cube side for a profiling run (default 256)')
+    ap.add_argument('--main-only', action='store_true', help='skip the secondary legs')
     a = ap.parse_args()
+    if a.box:
+        global BOX
+        BOX = (a.box, a.box, a.box)
     if a.impl == 'reference':
         ws, rank, _ = dist_env()
         if rank != 0:
             return 0
         a.steps = max(1, a.steps)
-        # per-step sample sized so the whole run stays within a few minutes
-        a.steps, a.warmup = a.steps, a.warmup
         out = run_reference(a, type('D', (), {'rank': 0, 'ws': ws})())
         print(json.dumps(out))
         return 0

@@ -215,6 +215,7 @@ struct sclbm_sim {
     FusedGeom fg = {};
     int fused_grid = 0, path = SCLBM_PATH_AUTO, chunk_override = 0;
     bool n_set = false, u_set = false, pop_set = false, moments_fresh = false;
+    bool dn_fresh = true;  // dn holds the density of the current populations
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int64_t device_bytes = 0;
     void *stage = nullptr;  // pinned host staging buffer (lazy)
@@ -581,6 +582,17 @@ int configure(sclbm_sim *s, int collision, double tau, const double *mrt_s, cons
     return SCLBM_OK;
 }
 
+// The single-pass kernel does not write the density array; readers of it
+// first reduce the current populations (the reference's n array holds the
+// density at the start of the last step; here it is always the current one).
+int ensure_density(sclbm_sim *s) {
+    if (s->dn_fresh || !s->pop_set) return SCLBM_OK;
+    cudaError_t e = s->ops->density(s->pop[s->cur], s->dn, s->psi, s->sp.data(), s->dgrid, s->st);
+    if (e != cudaSuccess) return fail(SCLBM_ERR_CUDA, "density: %s", cudaGetErrorString(e));
+    s->dn_fresh = true;
+    return SCLBM_OK;
+}
+
 }  // namespace
 
 // ============================================================================
@@ -741,7 +753,7 @@ int sclbm_set_density(sclbm_sim *s, const double *n) {
     DevGuard dg(s->device);
     double shift = s->rho0;
     int rc = h2d_real(s, s->dn, n, s->V, s->fp32 ? &shift : nullptr, s->V);
-    if (!rc) s->n_set = true;
+    if (!rc) s->n_set = s->dn_fresh = true;
     return rc;
 }
 
@@ -756,6 +768,8 @@ int sclbm_set_velocity(sclbm_sim *s, const double *u) {
 int sclbm_get_density(sclbm_sim *s, double *n) {
     if (!s || !n) return fail(SCLBM_ERR_ARG, "null argument");
     DevGuard dg(s->device);
+    int rc = ensure_density(s);
+    if (rc) return rc;
     double shift = s->rho0;
     return d2h_real(s, s->dn, n, s->V, s->fp32 ? &shift : nullptr, s->V);
 }
@@ -782,7 +796,7 @@ int sclbm_set_populations(sclbm_sim *s, const double *pop) {
     int rc = h2d_real(s, s->pop[s->cur], pop, s->V * s->Q, s->fp32 ? shift.data() : nullptr, s->V);
     if (!rc) {
         s->pop_set = true;
-        s->moments_fresh = false;
+        s->moments_fresh = s->dn_fresh = false;
     }
     return rc;
 }
@@ -812,7 +826,7 @@ int sclbm_step(sclbm_sim *s, int64_t nsteps) {
     if (nsteps < 0) return fail(SCLBM_ERR_ARG, "nsteps < 0");
     if (!s->pop_set) return fail(SCLBM_ERR_STATE, "populations are not initialized");
     DevGuard dg(s->device);
-    s->moments_fresh = false;
+    s->moments_fresh = s->dn_fresh = false;
     return run_steps(s, nsteps);
 }
 
@@ -838,7 +852,7 @@ int sclbm_step_timed(sclbm_sim *s, int64_t nsteps, double *ms) {
     cudaEventElapsedTime(&t, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    s->moments_fresh = false;
+    s->moments_fresh = s->dn_fresh = false;
     *ms = t;
     if (rc) return rc;
     CUDA_TRY(cudaGetLastError());
@@ -872,7 +886,7 @@ int sclbm_profile_step(sclbm_sim *s, int64_t nsteps, double *ms, int nms) {
         }
     }
     for (auto &e : ev) cudaEventDestroy(e);
-    s->moments_fresh = false;
+    s->moments_fresh = s->dn_fresh = false;
     if (rc) return rc;
     if (ce != cudaSuccess) return fail(SCLBM_ERR_CUDA, "profile: %s", cudaGetErrorString(ce));
     ms[0] = t0 / nsteps;  // density + psi pass (0 on the single-pass path)
@@ -914,7 +928,7 @@ int sclbm_compute_moments(sclbm_sim *s) {
     if (e != cudaSuccess) return fail(SCLBM_ERR_CUDA, "moments: %s", cudaGetErrorString(e));
     CUDA_TRY(cudaStreamSynchronize(s->st));
     s->n_set = s->u_set = true;
-    s->moments_fresh = true;
+    s->moments_fresh = s->dn_fresh = true;
     return SCLBM_OK;
 }
 
@@ -964,6 +978,10 @@ int sclbm_check_u(sclbm_sim *s, double *u_conv, double *max_u) {
 int sclbm_center_of_mass(sclbm_sim *s, double *mass, double *cm) {
     if (!s) return fail(SCLBM_ERR_ARG, "null handle");
     DevGuard dg(s->device);
+    {
+        int rc0 = ensure_density(s);
+        if (rc0) return rc0;
+    }
     if (s->fp32) k_com<float><<<s->red_blocks, RED_THREADS, 0, s->st>>>((const float *)s->dn, s->rho0, s->D, s->L[0], s->L[1], s->V, s->red);
     else k_com<double><<<s->red_blocks, RED_THREADS, 0, s->st>>>((const double *)s->dn, 0.0, s->D, s->L[0], s->L[1], s->V, s->red);
     std::vector<double> part;
@@ -981,6 +999,10 @@ int sclbm_center_of_mass(sclbm_sim *s, double *mass, double *cm) {
 int sclbm_density_at(sclbm_sim *s, const int64_t *idx, int count, double *out) {
     if (!s || !idx || !out || count < 0) return fail(SCLBM_ERR_ARG, "bad argument");
     DevGuard dg(s->device);
+    {
+        int rc0 = ensure_density(s);
+        if (rc0) return rc0;
+    }
     for (int i = 0; i < count; i++) {
         if (idx[i] < 0 || idx[i] >= s->V) return fail(SCLBM_ERR_ARG, "index %lld out of range", (long long)idx[i]);
         if (s->fp32) {
@@ -999,6 +1021,10 @@ int sclbm_density_at(sclbm_sim *s, const int64_t *idx, int count, double *out) {
 int sclbm_density_finite(sclbm_sim *s, int *finite, double *max_abs) {
     if (!s) return fail(SCLBM_ERR_ARG, "null handle");
     DevGuard dg(s->device);
+    {
+        int rc0 = ensure_density(s);
+        if (rc0) return rc0;
+    }
     if (s->fp32) k_finite<float><<<s->red_blocks, RED_THREADS, 0, s->st>>>((const float *)s->dn, s->rho0, s->V, s->red);
     else k_finite<double><<<s->red_blocks, RED_THREADS, 0, s->st>>>((const double *)s->dn, 0.0, s->V, s->red);
     std::vector<double> part;

@@ -376,3 +376,27 @@ def test_single_pass_fp32_close_to_fp64_short():
     assert rel_err(b.get_velocity(), a.get_velocity()) < 1e-4
     a.close()
     b.close()
+
+
+def test_density_readers_follow_the_single_pass_kernel():
+    """The single-pass kernel writes no density array; density read-backs,
+    the centre of mass and the finiteness check reduce the current populations."""
+    dims = (48, 40, 32)
+    x, f = XIStencils['D3Q19'], FStencils['D3E6']
+    n0 = droplet(dims, 9.0, 4.636, 0.147, 2.0, 8)
+    s = _lib.Sim(3, dims, x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], -4.5, precision=_lib.FP32_SHIFTED,
+                 rho0=1.0)
+    s.set_density(n0)
+    s.set_velocity(np.zeros(3 * s.V))
+    s.init_populations()
+    s.step(40)
+    pop = s.get_populations().reshape(19, -1)
+    n_pop = pop.sum(axis=0)
+    assert rel_err(s.get_density(), n_pop) < 1e-6
+    m, cm = s.center_of_mass()
+    assert abs(m - n_pop.sum()) / m < 1e-6
+    ok, mx = s.density_finite()
+    assert ok and abs(mx - n_pop.max()) / mx < 1e-6
+    idx = [0, 1234, s.V - 1]
+    np.testing.assert_allclose(s.density_at(idx), n_pop[idx], rtol=1e-6)
+    s.close()
