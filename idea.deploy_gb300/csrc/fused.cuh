@@ -94,183 +94,231 @@ __device__ __forceinline__ float bgk_fp32(const float *f, const float *u, const 
     return p.a_nonzero ? fmaf(p.A[q][q], f[q], rhs) : rhs;
 }
 
+// One work item: the tile (x0, y0) of one lattice, planes [m0, m1).  pop and
+// pop_out point at the lattice's first cell, V is the distance between two
+// populations of a cell (the lattice volume, or a batch's total volume).
+template <class L, class S, bool MRT>
+__device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float *__restrict__ pop_out, const int V,
+                                           const int Lx, const int Ly, const int Lz, const int x0, const int y0,
+                                           const int m0, const int m1, const float neg_g, const float rho0,
+                                           const StepParams<L, S, float> &p, float *smem) {
+    using SH = FusedShape<L, S>;
+    constexpr int D = L::D, Q = L::Q, R = SH::R, HX = SH::HX, HC = SH::HC, NT = SH::NT, RING = SH::RING;
+    float *ring = smem;  // psi ring [RING][HC], then (2D) 2 stage buffers [HPT][Q][NT]
+    float *stage0 = smem + RING * HC;
+    const int tid = threadIdx.x;
+    const int Lm = D == 3 ? Lz : Ly;       // marching extent
+    const int PL = D == 3 ? Lx * Ly : Lx;  // cells per plane
+    const int tx = tid % SH::TX, ty = D == 3 ? tid / SH::TX : 0;
+
+    // in-plane offsets of the halo cells this thread reduces (fixed per tile)
+    int hoff[SH::HPT];
+#pragma unroll
+    for (int k = 0; k < SH::HPT; k++) {
+        const int c = tid + k * NT;
+        const int hx = c % HX, hy = c / HX;
+        const int gx = wrapm(x0 - R + hx, Lx);
+        hoff[k] = D == 3 ? gx + Lx * wrapm(y0 - R + hy, Ly) : gx;
+    }
+    // interior cell of this thread and its wrapped neighbour columns / rows
+    const int x = x0 + tx, y = D == 3 ? y0 + ty : 0;
+    const bool in_tile = x < Lx && (D == 2 || y < Ly);
+    int X3[3], Y3[3];
+#pragma unroll
+    for (int o = -1; o <= 1; o++) {
+        X3[o + 1] = wrapc(x + o, Lx);
+        Y3[o + 1] = D == 3 ? Lx * wrapc(y + o, Ly) : 0;
+    }
+    const int own = X3[1] + Y3[1];
+
+    // n and psi of plane m straight from global memory; every load is issued
+    // before the first sum (threads without a second halo cell re-read their
+    // first one and skip the store), so HPT*Q loads are in flight at once
+    auto psi_plane = [&](int m) {
+        float *slot = ring + wrapm(m, RING) * HC;
+        const int poff = wrapm(m, Lm) * PL;
+        float v[SH::HPT][Q];
+#pragma unroll
+        for (int k = 0; k < SH::HPT; k++) {
+            const int c = tid + k * NT;
+            const float *src = pop + (poff + (c < HC ? hoff[k] : hoff[0]));
+#pragma unroll
+            for (int q = 0; q < Q; q++) v[k][q] = __ldg(src + q * V);
+        }
+#pragma unroll
+        for (int k = 0; k < SH::HPT; k++) {
+            const int c = tid + k * NT;
+            float s = v[k][lex_q<Q>(0)];
+#pragma unroll
+            for (int i = 1; i < Q; i++) s += v[k][lex_q<Q>(i)];
+            if (k + 1 < SH::HPT || c < HC) slot[c] = psi_fast(p.psi_kind, rho0 + s);
+        }
+    };
+    // asynchronous copy of this thread's halo populations of plane m into a stage buffer
+    auto stage_issue = [&](int m) {
+        float *st = stage0 + (m & 1) * SH::STAGE;
+        const int poff = wrapm(m, Lm) * PL;
+#pragma unroll
+        for (int k = 0; k < SH::HPT; k++) {
+            const int c = tid + k * NT;
+            if (k + 1 < SH::HPT || c < HC) {
+                const float *src = pop + (poff + hoff[k]);
+#pragma unroll
+                for (int q = 0; q < Q; q++) cp_async4(st + (k * Q + q) * NT + tid, src + q * V);
+            }
+        }
+        cp_async_commit();
+    };
+    // n and psi of plane m from the stage (each thread reads back only its own copies)
+    auto stage_reduce = [&](int m) {
+        const float *st = stage0 + (m & 1) * SH::STAGE;
+        float *slot = ring + wrapm(m, RING) * HC;
+#pragma unroll
+        for (int k = 0; k < SH::HPT; k++) {
+            const int c = tid + k * NT;
+            if (k + 1 < SH::HPT || c < HC) {
+                float s = st[(k * Q + lex_q<Q>(0)) * NT + tid];
+#pragma unroll
+                for (int i = 1; i < Q; i++) s += st[(k * Q + lex_q<Q>(i)) * NT + tid];
+                slot[c] = psi_fast(p.psi_kind, rho0 + s);
+            }
+        }
+    };
+
+    // 2D: the halo of plane m+R+1 is prefetched with cp.async during plane m;
+    // 3D: the halo (1.7x the tile) is reduced straight from L2 and the
+    // thread's own populations of plane m are loaded first, so both sets of
+    // loads are in flight together
+    constexpr bool STAGED = D == 2;
+    __syncthreads();  // the previous item's readers are done with the ring
+    for (int m = m0 - R; m < m0 + R; m++) psi_plane(m);
+    if (STAGED) stage_issue(m0 + R);
+    for (int m = m0; m < m1; m++) {
+        int Z3[3];
+#pragma unroll
+        for (int o = -1; o <= 1; o++) Z3[o + 1] = D == 3 ? wrapc(m + o, Lm) * PL : wrapc(m + o, Lm) * Lx;
+        const int g = own + Z3[1];
+        float f[Q];
+        if (in_tile) {
+#pragma unroll
+            for (int q = 0; q < Q; q++) f[q] = __ldg(pop + (g + q * V));
+        }
+        if (STAGED) {
+            if (m + 1 < m1) {
+                stage_issue(m + R + 1);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
+            stage_reduce(m + R);
+        } else {
+            psi_plane(m + R);
+        }
+        __syncthreads();
+        if (in_tile) {
+            // slot bases of planes m-R .. m+R, offset to this thread's halo position
+            const float *sb[RING];
+#pragma unroll
+            for (int k = 0; k < RING; k++) sb[k] = ring + wrapm(m + k - R, RING) * HC + ty * HX + tx;
+            float d = f[lex_q<Q>(0)];
+#pragma unroll
+            for (int i = 1; i < Q; i++) d += f[lex_q<Q>(i)];
+            // Shan-Chen force from the psi ring (compile-time offsets)
+            float F[D];
+#pragma unroll
+            for (int c = 0; c < D; c++) F[c] = 0.f;
+#pragma unroll
+            for (int a = 0; a < S::QE; a++) {
+                const int em = D == 3 ? S::e(a, 2) : S::e(a, 1);
+                const int ey = D == 3 ? S::e(a, 1) : 0;
+                const float ps = sb[em + R][(D == 3 ? (R + ey) * HX : 0) + R + S::e(a, 0)];
+#pragma unroll
+                for (int c = 0; c < D; c++)
+                    if (S::e(a, c) != 0) F[c] = fmaf(p.sw[a][c], ps, F[c]);
+            }
+            const float sc = neg_g * sb[R][(D == 3 ? R * HX : 0) + R];
+#pragma unroll
+            for (int c = 0; c < D; c++) F[c] *= sc;
+            const float n = rho0 + d;
+            float u[D];
+            velocity<L, float>(f, n, F, u);
+            // collision + push stream; rest population last, from mass conservation
+            float u2 = 0.f, uF = 0.f;
+#pragma unroll
+            for (int c = 0; c < D; c++) {
+                u2 = fmaf(u[c], u[c], u2);
+                uF = fmaf(u[c], F[c], uF);
+            }
+            const float C0 = p.omega * d - p.om15 * n * u2 - p.fd * uF;
+            const float a = p.om45 * n, b = p.om3 * n;
+            float rest_pop = d;
+#pragma unroll
+            for (int q = 1; q < Q; q++) {
+                float out;
+                if (MRT) collide_cell<L, S, true, float, false>(f, d, n, u, F, q, p, out);
+                else out = bgk_fp32<L, S>(f, u, F, q, p, C0, a, b);
+                rest_pop -= out;
+                const int dst = X3[L::xi(q, 0) + 1] + Y3[L::xi(q, 1) + 1] + Z3[L::xi(q, D - 1) + 1];
+                pop_out[dst + q * V] = out;
+            }
+            pop_out[g] = rest_pop;
+        }
+    }
+}
+
 template <class L, class S, bool MRT>
 __global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
     k_fused(const float *__restrict__ pop, float *__restrict__ pop_out, const __grid_constant__ StepParams<L, S, float> p,
             const FusedGeom fg) {
     using SH = FusedShape<L, S>;
-    constexpr int D = L::D, Q = L::Q, R = SH::R, HX = SH::HX, HC = SH::HC, NT = SH::NT, RING = SH::RING;
-    extern __shared__ float smem[];  // psi ring [RING][HC], then 2 stage buffers [HPT][Q][NT]
-    float *ring = smem;
-    float *stage0 = smem + RING * HC;
-    const int tid = threadIdx.x;
-    const int V = (int)fg.V;
-    const int Lx = fg.L[0], Ly = fg.L[1], Lz = fg.L[2];
-    const int Lm = D == 3 ? Lz : Ly;                 // marching extent
-    const int PL = D == 3 ? Lx * Ly : Lx;            // cells per plane
-    const int tx = tid % SH::TX, ty = D == 3 ? tid / SH::TX : 0;
-
+    constexpr int D = L::D;
+    extern __shared__ float smem[];
+    const int Lm = D == 3 ? fg.L[2] : fg.L[1];
     for (int item = blockIdx.x; item < fg.items; item += gridDim.x) {
         const int ix = item % fg.tiles_x;
         const int rest = item / fg.tiles_x;
         const int iy = D == 3 ? rest % fg.tiles_y : 0;
         const int ic = D == 3 ? rest / fg.tiles_y : rest;
-        const int x0 = ix * SH::TX, y0 = iy * SH::TY;
-        const int m0 = ic * fg.chunk, m1 = min(m0 + fg.chunk, Lm);
+        const int m0 = ic * fg.chunk;
+        fused_tile<L, S, MRT>(pop, pop_out, (int)fg.V, fg.L[0], fg.L[1], fg.L[2], ix * SH::TX, iy * SH::TY, m0,
+                              min(m0 + fg.chunk, Lm), p.neg_g, p.rho0, p, smem);
+    }
+}
 
-        // in-plane offsets of the halo cells this thread reduces (fixed per tile)
-        int hoff[SH::HPT];
-#pragma unroll
-        for (int k = 0; k < SH::HPT; k++) {
-            const int c = tid + k * NT;
-            const int hx = c % HX, hy = c / HX;
-            const int gx = wrapm(x0 - R + hx, Lx);
-            hoff[k] = D == 3 ? gx + Lx * wrapm(y0 - R + hy, Ly) : gx;
-        }
-        // interior cell of this thread and its wrapped neighbour columns / rows
-        const int x = x0 + tx, y = D == 3 ? y0 + ty : 0;
-        const bool in_tile = x < Lx && (D == 2 || y < Ly);
-        int X3[3], Y3[3];
-#pragma unroll
-        for (int o = -1; o <= 1; o++) {
-            X3[o + 1] = wrapc(x + o, Lx);
-            Y3[o + 1] = D == 3 ? Lx * wrapc(y + o, Ly) : 0;
-        }
-        const int own = X3[1] + Y3[1];
+// ---------------------------------------------------------------------------
+// Batches of independent lattices (ragged sweeps): the lattices sit one after
+// another in one SoA array (population q of cell g of lattice i at
+// q*Vtot + base_i + g); every lattice has its own size, coupling G and FP32
+// shift.  One launch steps every active lattice: CTAs take (lattice, tile,
+// chunk) work items from an atomic queue, so lattices of any size share the
+// GPU and retired lattices cost nothing.
+// ---------------------------------------------------------------------------
+struct BatchInst {
+    int base, Lx, Ly, Lz;
+    float neg_g, rho0;
+    int active, pad;
+};
 
-        // n and psi of plane m straight from global memory; every load is issued
-        // before the first sum (threads without a second halo cell re-read their
-        // first one and skip the store), so HPT*Q loads are in flight at once
-        auto psi_plane = [&](int m) {
-            float *slot = ring + wrapm(m, RING) * HC;
-            const int poff = wrapm(m, Lm) * PL;
-            float v[SH::HPT][Q];
-#pragma unroll
-            for (int k = 0; k < SH::HPT; k++) {
-                const int c = tid + k * NT;
-                const float *src = pop + (poff + (c < HC ? hoff[k] : hoff[0]));
-#pragma unroll
-                for (int q = 0; q < Q; q++) v[k][q] = __ldg(src + q * V);
-            }
-#pragma unroll
-            for (int k = 0; k < SH::HPT; k++) {
-                const int c = tid + k * NT;
-                float s = v[k][lex_q<Q>(0)];
-#pragma unroll
-                for (int i = 1; i < Q; i++) s += v[k][lex_q<Q>(i)];
-                if (k + 1 < SH::HPT || c < HC) slot[c] = psi_fast(p.psi_kind, p.rho0 + s);
-            }
-        };
-        // asynchronous copy of this thread's halo populations of plane m into a stage buffer
-        auto stage_issue = [&](int m) {
-            float *st = stage0 + (m & 1) * SH::STAGE;
-            const int poff = wrapm(m, Lm) * PL;
-#pragma unroll
-            for (int k = 0; k < SH::HPT; k++) {
-                const int c = tid + k * NT;
-                if (k + 1 < SH::HPT || c < HC) {
-                    const float *src = pop + (poff + hoff[k]);
-#pragma unroll
-                    for (int q = 0; q < Q; q++) cp_async4(st + (k * Q + q) * NT + tid, src + q * V);
-                }
-            }
-            cp_async_commit();
-        };
-        // n and psi of plane m from the stage (each thread reads back only its own copies)
-        auto stage_reduce = [&](int m) {
-            const float *st = stage0 + (m & 1) * SH::STAGE;
-            float *slot = ring + wrapm(m, RING) * HC;
-#pragma unroll
-            for (int k = 0; k < SH::HPT; k++) {
-                const int c = tid + k * NT;
-                if (k + 1 < SH::HPT || c < HC) {
-                    float s = st[(k * Q + lex_q<Q>(0)) * NT + tid];
-#pragma unroll
-                    for (int i = 1; i < Q; i++) s += st[(k * Q + lex_q<Q>(i)) * NT + tid];
-                    slot[c] = psi_fast(p.psi_kind, p.rho0 + s);
-                }
-            }
-        };
-
-        // 2D: the halo of plane m+R+1 is prefetched with cp.async during plane m;
-        // 3D: the halo (1.7x the tile) is reduced straight from L2 and the
-        // thread's own populations of plane m are loaded first, so both sets of
-        // loads are in flight together
-        constexpr bool STAGED = D == 2;
-        __syncthreads();  // the previous item's readers are done with the ring
-        for (int m = m0 - R; m < m0 + R; m++) psi_plane(m);
-        if (STAGED) stage_issue(m0 + R);
-        for (int m = m0; m < m1; m++) {
-            int Z3[3];
-#pragma unroll
-            for (int o = -1; o <= 1; o++) Z3[o + 1] = D == 3 ? wrapc(m + o, Lm) * PL : wrapc(m + o, Lm) * Lx;
-            const int g = own + Z3[1];
-            float f[Q];
-            if (in_tile) {
-#pragma unroll
-                for (int q = 0; q < Q; q++) f[q] = __ldg(pop + (g + q * V));
-            }
-            if (STAGED) {
-                if (m + 1 < m1) {
-                    stage_issue(m + R + 1);
-                    cp_async_wait<1>();
-                } else {
-                    cp_async_wait<0>();
-                }
-                stage_reduce(m + R);
-            } else {
-                psi_plane(m + R);
-            }
-            __syncthreads();
-            if (in_tile) {
-                // slot bases of planes m-R .. m+R, offset to this thread's halo position
-                const float *sb[RING];
-#pragma unroll
-                for (int k = 0; k < RING; k++) sb[k] = ring + wrapm(m + k - R, RING) * HC + ty * HX + tx;
-                float d = f[lex_q<Q>(0)];
-#pragma unroll
-                for (int i = 1; i < Q; i++) d += f[lex_q<Q>(i)];
-                // Shan-Chen force from the psi ring (compile-time offsets)
-                float F[D];
-#pragma unroll
-                for (int c = 0; c < D; c++) F[c] = 0.f;
-#pragma unroll
-                for (int a = 0; a < S::QE; a++) {
-                    const int em = D == 3 ? S::e(a, 2) : S::e(a, 1);
-                    const int ey = D == 3 ? S::e(a, 1) : 0;
-                    const float ps = sb[em + R][(D == 3 ? (R + ey) * HX : 0) + R + S::e(a, 0)];
-#pragma unroll
-                    for (int c = 0; c < D; c++)
-                        if (S::e(a, c) != 0) F[c] = fmaf(p.sw[a][c], ps, F[c]);
-                }
-                const float sc = p.neg_g * sb[R][(D == 3 ? R * HX : 0) + R];
-#pragma unroll
-                for (int c = 0; c < D; c++) F[c] *= sc;
-                const float n = p.rho0 + d;
-                float u[D];
-                velocity<L, float>(f, n, F, u);
-                // collision + push stream; rest population last, from mass conservation
-                float u2 = 0.f, uF = 0.f;
-#pragma unroll
-                for (int c = 0; c < D; c++) {
-                    u2 = fmaf(u[c], u[c], u2);
-                    uF = fmaf(u[c], F[c], uF);
-                }
-                const float C0 = p.omega * d - p.om15 * n * u2 - p.fd * uF;
-                const float a = p.om45 * n, b = p.om3 * n;
-                float rest_pop = d;
-#pragma unroll
-                for (int q = 1; q < Q; q++) {
-                    float out;
-                    if (MRT) collide_cell<L, S, true, float, false>(f, d, n, u, F, q, p, out);
-                    else out = bgk_fp32<L, S>(f, u, F, q, p, C0, a, b);
-                    rest_pop -= out;
-                    const int dst = X3[L::xi(q, 0) + 1] + Y3[L::xi(q, 1) + 1] + Z3[L::xi(q, D - 1) + 1];
-                    pop_out[dst + q * V] = out;
-                }
-                pop_out[g] = rest_pop;
-            }
-        }
+template <class L, class S, bool MRT>
+__global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
+    k_fused_batch(const float *__restrict__ pop, float *__restrict__ pop_out,
+                  const __grid_constant__ StepParams<L, S, float> p, const BatchInst *__restrict__ inst,
+                  const int4 *__restrict__ items, const int n_items, const int Vtot, int *counter, const int parity) {
+    extern __shared__ float smem[];
+    __shared__ int next;
+    // the other parity's queue is reset for the next step (not used by this one)
+    if (blockIdx.x == 0 && threadIdx.x == 0) counter[parity ^ 1] = 0;
+    while (true) {
+        if (threadIdx.x == 0) next = atomicAdd(&counter[parity], 1);
+        __syncthreads();
+        const int it = next;
+        __syncthreads();
+        if (it >= n_items) break;
+        const int4 w = items[it];  // lattice, x0, y0, m0 | m1 << 16
+        const BatchInst I = inst[w.x];
+        if (!I.active) continue;
+        fused_tile<L, S, MRT>(pop + I.base, pop_out + I.base, Vtot, I.Lx, I.Ly, I.Lz, w.y, w.z, w.w & 0xffff,
+                              w.w >> 16, I.neg_g, I.rho0, p, smem);
     }
 }
 

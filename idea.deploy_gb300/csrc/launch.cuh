@@ -9,6 +9,7 @@
 #include <cuda_runtime.h>
 #include <type_traits>
 
+#include "batch.cuh"
 #include "fused.cuh"
 #include "kernels.cuh"
 
@@ -50,6 +51,13 @@ struct KernelOps {
                          cudaStream_t st);
     int fused_tx, fused_ty, fused_r;
     int (*fused_occupancy)();
+    // batches of lattices (FP32 only, else null)
+    cudaError_t (*batch_step)(const void *pop, void *pop_out, const void *sp, const BatchInst *inst, const int4 *items,
+                              int n_items, int Vtot, int *counter, int parity, int grid, cudaStream_t st);
+    cudaError_t (*batch_density)(const void *pop, void *dn, void *psi, const void *sp, const BatchInst *inst, int n_inst,
+                                 int Vtot, int gx, cudaStream_t st);
+    cudaError_t (*batch_moments)(const void *pop, const void *dn, const void *psi, void *u_old, const void *sp,
+                                 const BatchInst *inst, int n_inst, int Vtot, double *partials, int gx, cudaStream_t st);
 };
 
 template <class L, class S, bool MRT, class Real, bool STRICT>
@@ -159,13 +167,54 @@ struct Ops {
         }
         return 0;
     }
+    static cudaError_t batch_step(const void *pop, void *pop_out, const void *sp, const BatchInst *inst,
+                                  const int4 *items, int n_items, int Vtot, int *counter, int parity, int grid,
+                                  cudaStream_t st) {
+        if constexpr (std::is_same<Real, float>::value) {
+            using SH = FusedShape<L, S>;
+            static bool done[64] = {};
+            int dev = 0;
+            cudaGetDevice(&dev);
+            if (dev < 0 || dev >= 64 || !done[dev]) {
+                cudaFuncSetAttribute(k_fused_batch<L, S, MRT>, cudaFuncAttributeMaxDynamicSharedMemorySize, SH::SMEM);
+                if (dev >= 0 && dev < 64) done[dev] = true;
+            }
+            k_fused_batch<L, S, MRT><<<grid, SH::NT, SH::SMEM, st>>>((const float *)pop, (float *)pop_out,
+                                                                     *static_cast<const SP *>(sp), inst, items,
+                                                                     n_items, Vtot, counter, parity);
+            return cudaGetLastError();
+        }
+        return cudaErrorNotSupported;
+    }
+    static cudaError_t batch_density(const void *pop, void *dn, void *psi, const void *sp, const BatchInst *inst,
+                                     int n_inst, int Vtot, int gx, cudaStream_t st) {
+        if constexpr (std::is_same<Real, float>::value) {
+            k_batch_density<L><<<dim3(gx, n_inst), BATCH_THREADS, 0, st>>>(
+                (const float *)pop, (float *)dn, (float *)psi, inst, Vtot, static_cast<const SP *>(sp)->psi_kind);
+            return cudaGetLastError();
+        }
+        return cudaErrorNotSupported;
+    }
+    static cudaError_t batch_moments(const void *pop, const void *dn, const void *psi, void *u_old, const void *sp,
+                                     const BatchInst *inst, int n_inst, int Vtot, double *partials, int gx,
+                                     cudaStream_t st) {
+        if constexpr (std::is_same<Real, float>::value) {
+            k_batch_moments<L, S><<<dim3(gx, n_inst), BATCH_THREADS, 0, st>>>(
+                (const float *)pop, (const float *)dn, (const float *)psi, (float *)u_old, *static_cast<const SP *>(sp),
+                inst, Vtot, partials);
+            return cudaGetLastError();
+        }
+        return cudaErrorNotSupported;
+    }
     static const KernelOps *ops() {
         constexpr bool f32 = std::is_same<Real, float>::value;
         using SH = FusedShape<L, S>;
         static const KernelOps o = {sizeof(SP), sizeof(EP), f32 ? 1 : 2, &fill_step, &fill_eq, &density,
                                     &fcs, &velocity, &init_pop, &grids,
                                     f32 ? &fused : nullptr, SH::TX, SH::TY, SH::R,
-                                    f32 ? &fused_occupancy : nullptr};
+                                    f32 ? &fused_occupancy : nullptr,
+                                    f32 ? &batch_step : nullptr, f32 ? &batch_density : nullptr,
+                                    f32 ? &batch_moments : nullptr};
         return &o;
     }
 };

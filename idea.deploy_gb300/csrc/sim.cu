@@ -1041,3 +1041,405 @@ int sclbm_density_finite(sclbm_sim *s, int *finite, double *max_abs) {
 }
 
 }  // extern "C"
+
+// ============================================================================
+// Batches of independent lattices (include/sclbm.h, sclbm_batch_*)
+// ============================================================================
+struct sclbm_batch {
+    int device = 0, sms = 1;
+    cudaStream_t st = nullptr;
+    int D = 0, Q = 0, order = 0, n = 0;
+    double c2 = 1.0 / 3;
+    int psi_kind = 0;
+    std::vector<int> sizes;
+    std::vector<double> w;
+    std::vector<BatchInst> inst;
+    BatchInst *inst_d = nullptr;
+    int64_t Vtot = 0;
+    std::vector<int4> items;
+    int4 *items_d = nullptr;
+    int *counter = nullptr;  // [2] work queues, one per step parity
+    float *wq_d = nullptr;
+    const KernelOps *ops = nullptr;
+    std::vector<unsigned char> sp;
+    void *pop[2] = {nullptr, nullptr};
+    int cur = 0;
+    void *dn = nullptr, *psi = nullptr, *u_old = nullptr;
+    double *partials = nullptr;
+    int gx = 1, grid = 1;
+    std::vector<int> home;  // buffer holding a retired lattice's state (-1 while active)
+    std::vector<int64_t> steps;
+    bool pop_set = false;
+    cudaGraphExec_t graph[2] = {nullptr, nullptr};
+    int64_t device_bytes = 0;
+};
+
+namespace {
+
+constexpr int BATCH_CHUNK = 32;     // planes per work item
+constexpr int BATCH_CHECK_BLOCKS = 32;  // blocks per lattice in the observable kernels
+
+int balloc(sclbm_batch *b, void **p, size_t bytes) {
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return fail(SCLBM_ERR_NOMEM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
+    }
+    b->device_bytes += (int64_t)bytes;
+    return SCLBM_OK;
+}
+
+void brelease(sclbm_batch *b) {
+    for (auto &g : b->graph)
+        if (g) cudaGraphExecDestroy(g), g = nullptr;
+    for (void *p : {b->pop[0], b->pop[1], b->dn, b->psi, b->u_old, (void *)b->partials, (void *)b->inst_d,
+                    (void *)b->items_d, (void *)b->counter, (void *)b->wq_d})
+        if (p) cudaFree(p);
+    if (b->st) cudaStreamDestroy(b->st);
+}
+
+int64_t lattice_cells(const sclbm_batch *b, int i) {
+    int64_t v = 1;
+    for (int d = 0; d < b->D; d++) v *= b->sizes[(size_t)i * b->D + d];
+    return v;
+}
+
+int batch_launch_step(sclbm_batch *b) {
+    cudaError_t e = b->ops->batch_step(b->pop[b->cur], b->pop[b->cur ^ 1], b->sp.data(), b->inst_d, b->items_d,
+                                       (int)b->items.size(), (int)b->Vtot, b->counter, b->cur, b->grid, b->st);
+    if (e != cudaSuccess) return fail(SCLBM_ERR_CUDA, "batch step: %s", cudaGetErrorString(e));
+    b->cur ^= 1;
+    return SCLBM_OK;
+}
+
+int batch_run(sclbm_batch *b, int64_t nsteps) {
+    // the queue of step s is counter[s parity]; a graph holds an even number of steps
+    while (nsteps >= GRAPH_STEPS) {
+        if (!b->graph[b->cur]) {
+            const int saved = b->cur;
+            cudaGraph_t g = nullptr;
+            CUDA_TRY(cudaStreamBeginCapture(b->st, cudaStreamCaptureModeThreadLocal));
+            int rc = SCLBM_OK;
+            for (int i = 0; i < GRAPH_STEPS && rc == SCLBM_OK; i++) rc = batch_launch_step(b);
+            cudaError_t ce = cudaStreamEndCapture(b->st, &g);
+            b->cur = saved;
+            if (rc) {
+                if (g) cudaGraphDestroy(g);
+                return rc;
+            }
+            if (ce != cudaSuccess) return fail(SCLBM_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+            ce = cudaGraphInstantiate(&b->graph[saved], g, 0);
+            cudaGraphDestroy(g);
+            if (ce != cudaSuccess) return fail(SCLBM_ERR_CUDA, "graph instantiate: %s", cudaGetErrorString(ce));
+        }
+        CUDA_TRY(cudaGraphLaunch(b->graph[b->cur], b->st));
+        nsteps -= GRAPH_STEPS;
+    }
+    for (int64_t i = 0; i < nsteps; i++) {
+        int rc = batch_launch_step(b);
+        if (rc) return rc;
+    }
+    return SCLBM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int sclbm_batch_create(const sclbm_params *p, int n, const int *sizes, const double *G, const double *rho0,
+                       sclbm_batch **out) {
+    g_err.clear();
+    if (!p || !out || !sizes || !G || !rho0 || n < 1) return fail(SCLBM_ERR_ARG, "bad argument");
+    *out = nullptr;
+    if (p->precision != SCLBM_FP32_SHIFTED) return fail(SCLBM_ERR_UNSUPPORTED, "batches use FP32-shifted storage");
+    if (p->dim != 2 && p->dim != 3) return fail(SCLBM_ERR_UNSUPPORTED, "dimension %d", p->dim);
+    if (!p->xi || !p->w || !p->e || !p->we) return fail(SCLBM_ERR_ARG, "null stencil table");
+    const int *cx = compiled_xi(p->dim, p->q);
+    if (!cx) return fail(SCLBM_ERR_UNSUPPORTED, "lattice D%dQ%d not built", p->dim, p->q);
+    for (int i = 0; i < p->q * p->dim; i++)
+        if (p->xi[i] != cx[i]) return fail(SCLBM_ERR_UNSUPPORTED, "lattice velocities differ");
+    const int order = stencil_order(p->dim, p->e, p->qe);
+    if (!order) return fail(SCLBM_ERR_UNSUPPORTED, "force stencil is not E4/E6/E8");
+    if (p->collision != SCLBM_COLL_BGK || !(p->tau > 0))
+        return fail(SCLBM_ERR_UNSUPPORTED, "batches run BGK with tau > 0");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(SCLBM_ERR_NODEVICE, "no CUDA device visible");
+    }
+    if (p->device < 0 || p->device >= ndev) return fail(SCLBM_ERR_ARG, "device %d", p->device);
+    int64_t Vtot = 0;
+    for (int i = 0; i < n; i++) {
+        int64_t v = 1;
+        for (int d = 0; d < p->dim; d++) {
+            const int L = sizes[(size_t)i * p->dim + d];
+            if (L < 2 || L > 32767) return fail(SCLBM_ERR_ARG, "lattice %d size %d out of range", i, L);
+            v *= L;
+        }
+        Vtot += v;
+    }
+    if ((int64_t)p->q * Vtot >= ((int64_t)1 << 31))
+        return fail(SCLBM_ERR_UNSUPPORTED, "batch too large: q * cells must stay below 2^31");
+
+    sclbm_batch *b = new sclbm_batch();
+    b->device = p->device;
+    DevGuard dg(b->device);
+    cudaDeviceProp prop;
+    cudaGetDeviceProperties(&prop, b->device);
+    b->sms = prop.multiProcessorCount;
+    b->D = p->dim;
+    b->Q = p->q;
+    b->order = order;
+    b->n = n;
+    b->c2 = p->c2;
+    b->psi_kind = p->psi_kind;
+    b->sizes.assign(sizes, sizes + (size_t)n * p->dim);
+    b->w.assign(p->w, p->w + p->q);
+    b->Vtot = Vtot;
+    b->ops = select_ops(p->dim, order, false, true, false);
+    b->home.assign(n, -1);
+    b->steps.assign(n, 0);
+    // lattices and work items (lattice-major so concurrent items are neighbours)
+    int64_t base = 0;
+    const int TX = b->ops->fused_tx, TY = b->ops->fused_ty;
+    for (int i = 0; i < n; i++) {
+        const int *L = &b->sizes[(size_t)i * b->D];
+        BatchInst I;
+        I.base = (int)base;
+        I.Lx = L[0];
+        I.Ly = L[1];
+        I.Lz = b->D == 3 ? L[2] : 1;
+        I.neg_g = (float)(-G[i]);
+        I.rho0 = (float)rho0[i];
+        I.active = 1;
+        I.pad = 0;
+        b->inst.push_back(I);
+        const int Lm = b->D == 3 ? I.Lz : I.Ly;
+        for (int m0 = 0; m0 < Lm; m0 += BATCH_CHUNK)
+            for (int y0 = 0; y0 < (b->D == 3 ? I.Ly : 1); y0 += TY)
+                for (int x0 = 0; x0 < I.Lx; x0 += TX)
+                    b->items.push_back(make_int4(i, x0, y0, m0 | (std::min(m0 + BATCH_CHUNK, Lm) << 16)));
+        base += lattice_cells(b, i);
+    }
+    // step parameters (BGK, FP32); G and rho0 come from the lattice table
+    CollisionSpec cs;
+    cs.dim = b->D;
+    cs.q = b->Q;
+    cs.xi = p->xi;
+    cs.w = p->w;
+    cs.c2 = p->c2;
+    cs.tau = p->tau;
+    cs.literals = SCLBM_LIT_EXACT;
+    CollisionTables t;
+    std::string err;
+    int rc = build_collision(cs, t, err) ? fail(SCLBM_ERR_UNSUPPORTED, "collision operator: %s", err.c_str())
+                                         : SCLBM_OK;
+    if (!rc) {
+        HostSetup h = {};
+        h.L[0] = h.L[1] = h.L[2] = 1;
+        h.V = Vtot;
+        h.psi_kind = p->psi_kind;
+        h.we = p->we;
+        h.A = t.A.data();
+        h.B = t.B.data();
+        h.Beq = t.Beq.data();
+        h.a_nonzero = t.A[0] != 0.0;
+        h.omega = 1.0 / p->tau;
+        h.w = p->w;
+        b->sp.assign(b->ops->step_size, 0);
+        b->ops->fill_step(b->sp.data(), h);
+    }
+    const size_t pb = (size_t)Vtot * b->Q * 4, fb = (size_t)Vtot * 4;
+    if (!rc && cudaStreamCreateWithFlags(&b->st, cudaStreamNonBlocking) != cudaSuccess)
+        rc = fail(SCLBM_ERR_CUDA, "stream create");
+    if (!rc) rc = balloc(b, &b->pop[0], pb);
+    if (!rc) rc = balloc(b, &b->pop[1], pb);
+    if (!rc) rc = balloc(b, &b->dn, fb);
+    if (!rc) rc = balloc(b, &b->psi, fb);
+    if (!rc) rc = balloc(b, &b->u_old, fb * b->D);
+    b->gx = BATCH_CHECK_BLOCKS;
+    if (!rc) rc = balloc(b, (void **)&b->partials, (size_t)n * b->gx * BATCH_NV * sizeof(double));
+    if (!rc) rc = balloc(b, (void **)&b->inst_d, sizeof(BatchInst) * n);
+    if (!rc) rc = balloc(b, (void **)&b->items_d, sizeof(int4) * b->items.size());
+    if (!rc) rc = balloc(b, (void **)&b->counter, 2 * sizeof(int));
+    if (!rc) rc = balloc(b, (void **)&b->wq_d, sizeof(float) * b->Q);
+    if (!rc) {
+        std::vector<float> wq(b->w.begin(), b->w.end());
+        if (cudaMemcpy(b->inst_d, b->inst.data(), sizeof(BatchInst) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemcpy(b->items_d, b->items.data(), sizeof(int4) * b->items.size(), cudaMemcpyHostToDevice) !=
+                cudaSuccess ||
+            cudaMemcpy(b->wq_d, wq.data(), sizeof(float) * b->Q, cudaMemcpyHostToDevice) != cudaSuccess ||
+            cudaMemset(b->counter, 0, 2 * sizeof(int)) != cudaSuccess ||
+            cudaMemset(b->u_old, 0, fb * b->D) != cudaSuccess || cudaMemset(b->dn, 0, fb) != cudaSuccess)
+            rc = fail(SCLBM_ERR_CUDA, "batch upload: %s", cudaGetErrorString(cudaGetLastError()));
+    }
+    if (!rc) {
+        const int occ = b->ops->fused_occupancy();
+        b->grid = std::max(1, std::min((int)b->items.size(), b->sms * occ));
+    }
+    if (rc) {
+        brelease(b);
+        delete b;
+        return rc;
+    }
+    *out = b;
+    return SCLBM_OK;
+}
+
+int sclbm_batch_destroy(sclbm_batch *b) {
+    if (!b) return SCLBM_OK;
+    {
+        DevGuard dg(b->device);
+        cudaStreamSynchronize(b->st);
+        brelease(b);
+    }
+    delete b;
+    return SCLBM_OK;
+}
+
+int sclbm_batch_info(const sclbm_batch *b, int64_t *cells, int64_t *device_bytes) {
+    if (!b) return fail(SCLBM_ERR_ARG, "null handle");
+    if (cells) *cells = b->Vtot;
+    if (device_bytes) *device_bytes = b->device_bytes;
+    return SCLBM_OK;
+}
+
+int sclbm_batch_set_density(sclbm_batch *b, int i, const double *n) {
+    if (!b || !n || i < 0 || i >= b->n) return fail(SCLBM_ERR_ARG, "bad argument");
+    DevGuard dg(b->device);
+    const int64_t V = lattice_cells(b, i);
+    std::vector<float> tmp(V);
+    for (int64_t g = 0; g < V; g++) tmp[g] = (float)(n[g] - (double)b->inst[i].rho0);
+    CUDA_TRY(cudaMemcpy((float *)b->dn + b->inst[i].base, tmp.data(), V * sizeof(float), cudaMemcpyHostToDevice));
+    return SCLBM_OK;
+}
+
+int sclbm_batch_init_populations(sclbm_batch *b) {
+    if (!b) return fail(SCLBM_ERR_ARG, "null handle");
+    DevGuard dg(b->device);
+    const dim3 grid(b->gx, b->n);
+    if (b->D == 2)
+        k_batch_init<D2Q9><<<grid, BATCH_THREADS, 0, b->st>>>((float *)b->pop[b->cur], (const float *)b->dn, b->inst_d,
+                                                             (int)b->Vtot, b->wq_d);
+    else
+        k_batch_init<D3Q19><<<grid, BATCH_THREADS, 0, b->st>>>((float *)b->pop[b->cur], (const float *)b->dn, b->inst_d,
+                                                              (int)b->Vtot, b->wq_d);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(b->st));
+    b->pop_set = true;
+    return SCLBM_OK;
+}
+
+int sclbm_batch_step(sclbm_batch *b, int64_t nsteps) {
+    if (!b) return fail(SCLBM_ERR_ARG, "null handle");
+    if (!b->pop_set) return fail(SCLBM_ERR_STATE, "populations are not initialized");
+    if (nsteps < 0) return fail(SCLBM_ERR_ARG, "nsteps < 0");
+    DevGuard dg(b->device);
+    int rc = batch_run(b, nsteps);
+    if (!rc)
+        for (int i = 0; i < b->n; i++)
+            if (b->home[i] < 0) b->steps[i] += nsteps;
+    return rc;
+}
+
+int sclbm_batch_step_timed(sclbm_batch *b, int64_t nsteps, double *ms) {
+    if (!b || !ms) return fail(SCLBM_ERR_ARG, "bad argument");
+    DevGuard dg(b->device);
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    cudaEventRecord(e0, b->st);
+    int rc = sclbm_batch_step(b, nsteps);
+    cudaEventRecord(e1, b->st);
+    cudaEventSynchronize(e1);
+    float t = 0;
+    cudaEventElapsedTime(&t, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *ms = t;
+    if (rc) return rc;
+    CUDA_TRY(cudaGetLastError());
+    return SCLBM_OK;
+}
+
+int sclbm_batch_check(sclbm_batch *b, double *u_conv, double *max_u, double *mass) {
+    if (!b) return fail(SCLBM_ERR_ARG, "null handle");
+    if (!b->pop_set) return fail(SCLBM_ERR_STATE, "populations are not initialized");
+    DevGuard dg(b->device);
+    cudaError_t e = b->ops->batch_density(b->pop[b->cur], b->dn, b->psi, b->sp.data(), b->inst_d, b->n, (int)b->Vtot,
+                                          b->gx, b->st);
+    if (e == cudaSuccess)
+        e = b->ops->batch_moments(b->pop[b->cur], b->dn, b->psi, b->u_old, b->sp.data(), b->inst_d, b->n,
+                                  (int)b->Vtot, b->partials, b->gx, b->st);
+    if (e != cudaSuccess) return fail(SCLBM_ERR_CUDA, "batch check: %s", cudaGetErrorString(e));
+    std::vector<double> part((size_t)b->n * b->gx * BATCH_NV);
+    CUDA_TRY(cudaMemcpyAsync(part.data(), b->partials, part.size() * sizeof(double), cudaMemcpyDeviceToHost, b->st));
+    CUDA_TRY(cudaStreamSynchronize(b->st));
+    for (int i = 0; i < b->n; i++) {
+        if (b->home[i] >= 0) continue;  // retired: keep the caller's last values
+        double du = 0, mx = 0, m = 0;
+        for (int k = 0; k < b->gx; k++) {
+            const double *v = &part[((size_t)i * b->gx + k) * BATCH_NV];
+            du += v[0];
+            mx = std::max(mx, v[1]);
+            m += v[2];
+        }
+        const double V = (double)lattice_cells(b, i);
+        if (u_conv) u_conv[i] = du / V;
+        if (max_u) max_u[i] = std::sqrt(mx / b->c2);
+        if (mass) mass[i] = m;
+    }
+    return SCLBM_OK;
+}
+
+int sclbm_batch_set_active(sclbm_batch *b, const int *active) {
+    if (!b || !active) return fail(SCLBM_ERR_ARG, "bad argument");
+    DevGuard dg(b->device);
+    CUDA_TRY(cudaStreamSynchronize(b->st));
+    for (int i = 0; i < b->n; i++) {
+        const bool on = active[i] != 0;
+        if (!on && b->home[i] < 0) b->home[i] = b->cur;  // its state stays in this buffer
+        if (on && b->home[i] >= 0) {
+            // resuming: bring its state into the current buffer
+            if (b->home[i] != b->cur) {
+                const int64_t V = lattice_cells(b, i);
+                for (int q = 0; q < b->Q; q++)
+                    CUDA_TRY(cudaMemcpyAsync((float *)b->pop[b->cur] + (int64_t)q * b->Vtot + b->inst[i].base,
+                                             (const float *)b->pop[b->home[i]] + (int64_t)q * b->Vtot +
+                                                 b->inst[i].base,
+                                             V * sizeof(float), cudaMemcpyDeviceToDevice, b->st));
+            }
+            b->home[i] = -1;
+        }
+        b->inst[i].active = on ? 1 : 0;
+    }
+    CUDA_TRY(cudaMemcpyAsync(b->inst_d, b->inst.data(), sizeof(BatchInst) * b->n, cudaMemcpyHostToDevice, b->st));
+    CUDA_TRY(cudaStreamSynchronize(b->st));
+    return SCLBM_OK;
+}
+
+int sclbm_batch_get_density(sclbm_batch *b, int i, double *n) {
+    if (!b || !n || i < 0 || i >= b->n) return fail(SCLBM_ERR_ARG, "bad argument");
+    DevGuard dg(b->device);
+    CUDA_TRY(cudaStreamSynchronize(b->st));
+    const int64_t V = lattice_cells(b, i);
+    const int buf = b->home[i] >= 0 ? b->home[i] : b->cur;
+    std::vector<float> tmp(V);
+    for (int64_t g = 0; g < V; g++) n[g] = b->inst[i].rho0;
+    for (int i2 = 0; i2 < b->Q; i2++) {
+        const int q = b->Q > 10 ? (int[]){0, 1, 10, 11, 12, 13, 14, 15, 16, 17, 18, 2, 3, 4, 5, 6, 7, 8, 9}[i2] : i2;
+        CUDA_TRY(cudaMemcpy(tmp.data(), (const float *)b->pop[buf] + (int64_t)q * b->Vtot + b->inst[i].base,
+                            V * sizeof(float), cudaMemcpyDeviceToHost));
+        for (int64_t g = 0; g < V; g++) n[g] += (double)tmp[g];
+    }
+    return SCLBM_OK;
+}
+
+int sclbm_batch_steps(const sclbm_batch *b, int64_t *steps) {
+    if (!b || !steps) return fail(SCLBM_ERR_ARG, "bad argument");
+    for (int i = 0; i < b->n; i++) steps[i] = b->steps[i];
+    return SCLBM_OK;
+}
+
+}  // extern "C"

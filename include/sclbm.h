@@ -186,6 +186,42 @@ SCLBM_API int sclbm_density_at(sclbm_sim *s, const int64_t *idx, int count, doub
 /* 1 if every density value is finite, else 0 (max |n| also returned) */
 SCLBM_API int sclbm_density_finite(sclbm_sim *s, int *finite, double *max_abs);
 
+/* ---------------------------------------------------------------------------
+ * Batches: many independent periodic lattices of different sizes (ragged
+ * droplet sweeps), FP32-shifted storage, stepped together by one launch per
+ * step (CTAs take work items from a device queue, so retired lattices cost
+ * nothing).  No counterpart in the reference, which runs one
+ * ShanChenMultiPhase object per droplet (idpy/LBM/MultiPhase.py:140); each
+ * lattice follows the same step as sclbm_step.
+ * ------------------------------------------------------------------------- */
+typedef struct sclbm_batch sclbm_batch;
+
+/* p gives the lattice, stencil, psi, collision and device (sizes, sc_g and
+ * rho0 unused; precision must be SCLBM_FP32_SHIFTED); lattice i has sizes
+ * sizes[i*dim ..], coupling G[i] and shift rho0[i]. */
+SCLBM_API int sclbm_batch_create(const sclbm_params *p, int n, const int *sizes, const double *G,
+                                 const double *rho0, sclbm_batch **out);
+SCLBM_API int sclbm_batch_destroy(sclbm_batch *b);
+/* total cells and device bytes */
+SCLBM_API int sclbm_batch_info(const sclbm_batch *b, int64_t *cells, int64_t *device_bytes);
+/* density of lattice i (its own x-fastest layout); velocity starts at zero */
+SCLBM_API int sclbm_batch_set_density(sclbm_batch *b, int i, const double *n);
+SCLBM_API int sclbm_batch_get_density(sclbm_batch *b, int i, double *n);
+/* equilibrium populations of every lattice from its density (u = 0) */
+SCLBM_API int sclbm_batch_init_populations(sclbm_batch *b);
+/* enqueue nsteps steps of every active lattice (returns without waiting) */
+SCLBM_API int sclbm_batch_step(sclbm_batch *b, int64_t nsteps);
+SCLBM_API int sclbm_batch_step_timed(sclbm_batch *b, int64_t nsteps, double *ms);
+/* per active lattice: u_conv (sum |u - u_old| / V since the last check, the
+ * reference's CheckUConvergenceSCMP measure), max_u = sqrt(max|u|^2 / c2) and
+ * mass (FP64 reductions); u_old is then updated.  Retired lattices keep their
+ * last values. */
+SCLBM_API int sclbm_batch_check(sclbm_batch *b, double *u_conv, double *max_u, double *mass);
+/* retire (0) or keep (1) lattices; a retired lattice is no longer stepped */
+SCLBM_API int sclbm_batch_set_active(sclbm_batch *b, const int *active);
+/* steps each lattice has taken */
+SCLBM_API int sclbm_batch_steps(const sclbm_batch *b, int64_t *steps);
+
 #ifdef __cplusplus
 }
 #endif
