@@ -81,6 +81,17 @@ SIGNATURES = {
     'sclbm_center_of_mass': [_P, _DP, _DP],
     'sclbm_density_at': [_P, _I64P, ctypes.c_int, _DP],
     'sclbm_density_finite': [_P, _IP, _DP],
+    'sclbm_batch_create': [ctypes.POINTER(Params), ctypes.c_int, _P, _P, _P, ctypes.POINTER(_P)],
+    'sclbm_batch_destroy': [_P],
+    'sclbm_batch_info': [_P, _I64P, _I64P],
+    'sclbm_batch_set_density': [_P, ctypes.c_int, _P],
+    'sclbm_batch_get_density': [_P, ctypes.c_int, _P],
+    'sclbm_batch_init_populations': [_P],
+    'sclbm_batch_step': [_P, _I64],
+    'sclbm_batch_step_timed': [_P, _I64, _DP],
+    'sclbm_batch_check': [_P, _P, _P, _P],
+    'sclbm_batch_set_active': [_P, _P],
+    'sclbm_batch_steps': [_P, _P],
 }
 _STR = {'sclbm_version', 'sclbm_status_string', 'sclbm_last_error'}
 
