@@ -424,8 +424,47 @@ def run_reference(a, dist):
     return out
 
 
+def run_sweep_mode(a):
+    """Ragged droplet sweep (64 D2Q9 E8 droplets, R = 8..71): batched FP32 vs
+    the plain FP64 path, time to converge and Laplace-pressure error."""
+    from sclbm import sweep
+    r = sweep.run_sweep(n=a.sweep_n, max_steps=a.sweep_max_steps, plain=not a.no_plain)
+    b = r['batch']
+    out = {'metric': 'D2Q9 E8 droplet sweep: time to converge, batched FP32 vs plain FP64', 'unit': 's',
+           'config': r['config'], 'coexistence_wall_s': round(r['coexistence_wall_s'], 2),
+           'unstable': r['unstable'],
+           'batch': {'wall_s': round(b['wall_s'], 3), 'cells': int(sum(L * L for L in b['boxes'])),
+                     'status': {s: int((b['status'] == s).sum()) for s in set(b['status'])},
+                     'steps_max': int(b['steps'].max()), 'steps_mean': float(b['steps'].mean())}}
+    rows = []
+    for j in range(len(b['radii'])):
+        row = {'R': int(b['radii'][j]), 'L': int(b['boxes'][j]), 'G': round(float(b['G'][j]), 4),
+               'rho_l': round(r['coexistence'][j]['rho_l'], 6), 'rho_g': round(r['coexistence'][j]['rho_g'], 6),
+               'steps32': int(b['steps'][j]), 'status32': str(b['status'][j]), 'dp32': float(b['dp'][j])}
+        if 'plain' in r:
+            p = r['plain'][j]
+            row.update(steps64=int(p['steps']), status64=p['status'], dp64=float(p['dp']),
+                       dp_rel_err=float(abs(b['dp'][j] - p['dp']) / max(abs(p['dp']), 1e-300)))
+        rows.append(row)
+    out['droplets'] = rows
+    if 'plain' in r:
+        errs = np.array([x['dp_rel_err'] for x in rows if x['status32'] == 'converged'
+                         and x['status64'] == 'converged'])
+        out['plain'] = {'wall_s': round(r['plain_wall_s'], 3),
+                        'status': {s: sum(1 for x in rows if x['status64'] == s) for s in
+                                   set(x['status64'] for x in rows)}}
+        out['speedup_wall'] = round(r['plain_wall_s'] / b['wall_s'], 2)
+        out['dp_rel_err'] = {'max': float(errs.max()) if errs.size else None,
+                             'median': float(np.median(errs)) if errs.size else None, 'n': int(errs.size)}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument('--sweep', action='store_true', help='run the ragged droplet sweep instead')
+    ap.add_argument('--sweep-n', type=int, default=64)
+    ap.add_argument('--sweep-max-steps', type=int, default=100000)
+    ap.add_argument('--no-plain', action='store_true')
     ap.add_argument('--gpus', type=int, default=1)
     ap.add_argument('--steps', type=int, default=2000)
     ap.add_argument('--warmup', type=int, default=5)
@@ -439,6 +478,9 @@ def main():
     if a.box:
         global BOX
         BOX = (a.box, a.box, a.box)
+    if a.sweep:
+        print(json.dumps(run_sweep_mode(a)))
+        return 0
     if a.impl == 'reference':
         ws, rank, _ = dist_env()
         if rank != 0:
