@@ -6,6 +6,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -1443,3 +1444,124 @@ int sclbm_batch_steps(const sclbm_batch *b, int64_t *steps) {
 }
 
 }  // extern "C"
+
+// ============================================================================
+// One step with no device allocation (sclbm_step_noalloc).  The density+psi
+// pass and the force+collide+stream pass need two scratch fields (density and
+// psi, one value per cell) between them; here they live in a fixed array in the
+// library's own device data, so the call allocates nothing.  The array is
+// FP64-sized and split in two halves: the density at offset 0 and psi at
+// offset SCLBM_NOALLOC_MAX_CELLS * 8 bytes (FP32 fields use the first half of
+// each).  Every cell of both fields is written by the first pass before the
+// second pass reads it, so nothing has to be cleared between calls.
+static __device__ __align__(256) double g_noalloc_scratch[2 * (size_t)SCLBM_NOALLOC_MAX_CELLS];
+
+namespace {
+
+constexpr int NOALLOC_MAX_DEVICES = 64;
+std::mutex g_noalloc_mu;
+void *g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
+
+// device address of the scratch array on the current device (looked up once
+// per device; the host-side symbol itself is not a device address)
+int noalloc_scratch(int dev, void **out) {
+    if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return fail(SCLBM_ERR_ARG, "device %d beyond %d", dev, NOALLOC_MAX_DEVICES);
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    if (!g_noalloc_addr[dev]) {
+        void *p = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p) {
+            cudaGetLastError();
+            return fail(SCLBM_ERR_CUDA, "cudaGetSymbolAddress(scratch) on device %d: %s", dev, cudaGetErrorString(e));
+        }
+        g_noalloc_addr[dev] = p;
+    }
+    *out = g_noalloc_addr[dev];
+    return SCLBM_OK;
+}
+
+}  // namespace
+
+extern "C" int sclbm_step_noalloc(const sclbm_params *p, const void *pop_in, void *pop_out, void *stream) {
+    g_err.clear();
+    if (!p || !pop_in || !pop_out) return fail(SCLBM_ERR_ARG, "null argument");
+    if (p->dim != 2 && p->dim != 3) return fail(SCLBM_ERR_UNSUPPORTED, "dimension %d (2 or 3 supported)", p->dim);
+    if (!p->xi || !p->w || !p->e || !p->we) return fail(SCLBM_ERR_ARG, "null stencil table");
+    const int *cx = compiled_xi(p->dim, p->q);
+    if (!cx) return fail(SCLBM_ERR_UNSUPPORTED, "lattice D%dQ%d not built (D2Q9, D3Q19)", p->dim, p->q);
+    for (int i = 0; i < p->q * p->dim; i++)
+        if (p->xi[i] != cx[i]) return fail(SCLBM_ERR_UNSUPPORTED, "lattice velocities differ from D%dQ%d", p->dim, p->q);
+    const int order = stencil_order(p->dim, p->e, p->qe);
+    if (!order) return fail(SCLBM_ERR_UNSUPPORTED, "force stencil (%d vectors) is not E4/E6/E8", p->qe);
+    int64_t V = 1;
+    for (int d = 0; d < p->dim; d++) {
+        if (p->sizes[d] < 2 || p->sizes[d] > (1 << 24))
+            return fail(SCLBM_ERR_ARG, "size[%d] = %d out of range [2, 2^24]", d, p->sizes[d]);
+        V *= p->sizes[d];
+    }
+    if (V > SCLBM_NOALLOC_MAX_CELLS)
+        return fail(SCLBM_ERR_ARG, "lattice of %lld cells exceeds the %d-cell scratch of sclbm_step_noalloc "
+                    "(use a handle from sclbm_create)", (long long)V, SCLBM_NOALLOC_MAX_CELLS);
+    if (p->psi_kind < 0 || p->psi_kind > 2) return fail(SCLBM_ERR_ARG, "psi_kind %d", p->psi_kind);
+    if (p->precision != SCLBM_FP64 && p->precision != SCLBM_FP32_SHIFTED)
+        return fail(SCLBM_ERR_ARG, "precision %d", p->precision);
+    if (!(p->c2 > 0)) return fail(SCLBM_ERR_ARG, "c2 must be > 0");
+    const size_t rs = p->precision == SCLBM_FP32_SHIFTED ? 4 : 8;
+    const size_t bytes = (size_t)V * p->q * rs;
+    const char *a = (const char *)pop_in, *b = (const char *)pop_out;
+    if (a < b + bytes && b < a + bytes) return fail(SCLBM_ERR_ARG, "pop_in and pop_out overlap");
+
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+        cudaGetLastError();
+        return fail(SCLBM_ERR_NODEVICE, "no CUDA device visible");
+    }
+    if (p->device < 0 || p->device >= ndev) return fail(SCLBM_ERR_ARG, "device %d of %d", p->device, ndev);
+    int major = 0, sms = 0;
+    if (cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, p->device) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, p->device) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(SCLBM_ERR_CUDA, "device attributes");
+    }
+    if (major < 10) return fail(SCLBM_ERR_NODEVICE, "device %d is sm_%dx; built for sm_103a", p->device, major);
+    DevGuard dg(p->device);
+    void *scratch = nullptr;
+    {
+        int rc = noalloc_scratch(p->device, &scratch);
+        if (rc) return rc;
+    }
+    // host-side configuration only: the same kernel set, launch parameters and
+    // grids as a handle with these parameters (configure() touches no device memory)
+    sclbm_sim s;
+    s.device = p->device;
+    s.D = p->dim;
+    s.Q = p->q;
+    s.QE = p->qe;
+    s.order = order;
+    s.V = V;
+    for (int d = 0; d < s.D; d++) s.L[d] = p->sizes[d];
+    s.fp32 = p->precision == SCLBM_FP32_SHIFTED;
+    s.rs = rs;
+    s.rho0 = s.fp32 ? p->rho0 : 0.0;
+    s.c2 = p->c2;
+    s.G = p->sc_g;
+    s.psi_kind = p->psi_kind;
+    s.literals = p->literals;
+    s.sms = sms;
+    s.path = SCLBM_PATH_TWO_PASS;
+    s.w.assign(p->w, p->w + p->q);
+    s.we.assign(p->we, p->we + p->qe);
+    s.xi.assign(p->xi, p->xi + p->q * p->dim);
+    s.e.assign(p->e, p->e + p->qe * p->dim);
+    {
+        int rc = configure(&s, p->collision, p->tau, p->mrt_s, p->coll_a, p->coll_b);
+        if (rc) return rc;
+    }
+    void *dn = scratch;
+    void *psi = (char *)scratch + (size_t)SCLBM_NOALLOC_MAX_CELLS * sizeof(double);
+    cudaStream_t st = (cudaStream_t)stream;
+    cudaError_t e = s.ops->density(pop_in, dn, psi, s.sp.data(), s.dgrid, st);
+    if (e == cudaSuccess) e = s.ops->fcs(pop_in, pop_out, dn, psi, s.sp.data(), s.fgrid, st);
+    if (e != cudaSuccess) return fail(SCLBM_ERR_CUDA, "step launch: %s", cudaGetErrorString(e));
+    return SCLBM_OK;
+}

@@ -92,6 +92,7 @@ SIGNATURES = {
     'sclbm_batch_check': [_P, _P, _P, _P],
     'sclbm_batch_set_active': [_P, _P],
     'sclbm_batch_steps': [_P, _P],
+    'sclbm_step_noalloc': [ctypes.POINTER(Params), _P, _P, _P],
 }
 _STR = {'sclbm_version', 'sclbm_status_string', 'sclbm_last_error'}
 

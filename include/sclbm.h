@@ -222,6 +222,39 @@ SCLBM_API int sclbm_batch_set_active(sclbm_batch *b, const int *active);
 /* steps each lattice has taken */
 SCLBM_API int sclbm_batch_steps(const sclbm_batch *b, int64_t *steps);
 
+/* ---------------------------------------------------------------------------
+ * One step that allocates no device memory.  No counterpart in the reference.
+ *
+ * For callers that cannot let this library call cudaMalloc: a host program
+ * that reserves its whole device-memory budget once, in its own pool, and has
+ * no way to hand a handle's allocations to it; or a service in which an
+ * allocation or free during stepping (cudaFree synchronizes the device) would
+ * stall its other streams.  Such a caller keeps the populations in buffers it
+ * already owns and calls this instead of sclbm_create + sclbm_step.
+ *
+ * p describes the lattice exactly as for sclbm_create (sizes, stencils, G,
+ * psi, collision, precision, rho0, literals, device).  pop_in and pop_out are
+ * device pointers to q * V values each, q-major with x fastest, in the
+ * storage of p->precision (FP64: f; FP32_SHIFTED: float f - w_q rho0); they
+ * must not overlap.  One call enqueues one step (the density+psi pass and the
+ * force+collide+stream pass, the same kernels as a handle on
+ * SCLBM_PATH_TWO_PASS) on `stream` (a cudaStream_t; NULL = the legacy default
+ * stream) and returns without waiting; the caller swaps the buffers between
+ * calls.
+ *
+ * The scratch between the two passes (density and psi) is a fixed array in
+ * the library's device data, 16 MiB, held on every GPU that loads the library
+ * until the process exits.  Lattices of more than SCLBM_NOALLOC_MAX_CELLS
+ * cells are rejected with SCLBM_ERR_ARG.  All calls on one device share that
+ * device's copy of the array, which keeps the last call's contents, so calls
+ * whose kernels overlap on the GPU (streams with no ordering between them)
+ * race: order them on one stream.  The first
+ * call on each device looks up the array's device address (set-up done once
+ * per device); make that first call before any stream capture.
+ * ------------------------------------------------------------------------- */
+#define SCLBM_NOALLOC_MAX_CELLS (1 << 20)
+SCLBM_API int sclbm_step_noalloc(const sclbm_params *p, const void *pop_in, void *pop_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
