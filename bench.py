@@ -426,36 +426,56 @@ def run_reference(a, dist):
 
 def run_sweep_mode(a):
     """Ragged droplet sweep (64 D2Q9 E8 droplets, R = 8..71): batched FP32 vs
-    the plain FP64 path, time to converge and Laplace-pressure error."""
+    the plain FP64 path, time to converge and Laplace-pressure error; plus the
+    flat-interface densities against the thermodynamic construction and a
+    Laplace fit of the surface tension."""
     from sclbm import sweep
     r = sweep.run_sweep(n=a.sweep_n, max_steps=a.sweep_max_steps, plain=not a.no_plain)
     b = r['batch']
+    coex = []
+    for c in r['coexistence']:
+        row = {k: (round(v, 6) if isinstance(v, float) else v) for k, v in c.items()}
+        if c['status'] != 'diverged' and c['thermo_rho_l']:
+            row['rel_dev_thermo'] = [round(c['rho_l'] / c['thermo_rho_l'] - 1, 5),
+                                     round(c['rho_g'] / c['thermo_rho_g'] - 1, 5)]
+        coex.append(row)
     out = {'metric': 'D2Q9 E8 droplet sweep: time to converge, batched FP32 vs plain FP64', 'unit': 's',
            'config': r['config'], 'coexistence_wall_s': round(r['coexistence_wall_s'], 2),
-           'unstable': r['unstable'],
+           'coexistence': coex, 'unstable': r['unstable'],
            'batch': {'wall_s': round(b['wall_s'], 3), 'cells': int(sum(L * L for L in b['boxes'])),
                      'status': {s: int((b['status'] == s).sum()) for s in set(b['status'])},
                      'steps_max': int(b['steps'].max()), 'steps_mean': float(b['steps'].mean())}}
     rows = []
     for j in range(len(b['radii'])):
         row = {'R': int(b['radii'][j]), 'L': int(b['boxes'][j]), 'G': round(float(b['G'][j]), 4),
-               'rho_l': round(r['coexistence'][j]['rho_l'], 6), 'rho_g': round(r['coexistence'][j]['rho_g'], 6),
-               'steps32': int(b['steps'][j]), 'status32': str(b['status'][j]), 'dp32': float(b['dp'][j])}
-        if 'plain' in r:
-            p = r['plain'][j]
+               'rho_l': round(r['rho_l'][j], 6), 'rho_g': round(r['rho_g'][j], 6), 'rho_from': r['rho_source'][j],
+               'steps32': int(b['steps'][j]), 'status32': str(b['status'][j]), 'dp32': float(b['dp'][j]),
+               'max_u32': float(b['max_u'][j])}
+        p = r['plain'][j] if 'plain' in r else None
+        if p is not None:
             row.update(steps64=int(p['steps']), status64=p['status'], dp64=float(p['dp']),
+                       max_u64=float(p['max_u']), wall64_s=round(p['wall_s'], 3),
+                       steps64_dp_criterion=p['steps_dp'],
                        dp_rel_err=float(abs(b['dp'][j] - p['dp']) / max(abs(p['dp']), 1e-300)))
         rows.append(row)
     out['droplets'] = rows
     if 'plain' in r:
-        errs = np.array([x['dp_rel_err'] for x in rows if x['status32'] == 'converged'
-                         and x['status64'] == 'converged'])
+        both = [x for x in rows if x['status32'] == 'converged' and x.get('status64') == 'converged']
+        errs = np.array([x['dp_rel_err'] for x in both])
         out['plain'] = {'wall_s': round(r['plain_wall_s'], 3),
-                        'status': {s: sum(1 for x in rows if x['status64'] == s) for s in
-                                   set(x['status64'] for x in rows)}}
+                        'status': {s: sum(1 for x in rows if x.get('status64') == s) for s in
+                                   set(x.get('status64') for x in rows if 'status64' in x)}}
         out['speedup_wall'] = round(r['plain_wall_s'] / b['wall_s'], 2)
+        # the plain runs stopped at the batch's own criterion instead (where it fired)
+        wdp = sum((p['wall_dp_s'] if p['wall_dp_s'] is not None else p['wall_s'])
+                  for p in r['plain'] if p is not None)
+        out['plain']['wall_same_criterion_s'] = round(wdp, 3)
+        out['speedup_wall_same_criterion'] = round(wdp / b['wall_s'], 2)
         out['dp_rel_err'] = {'max': float(errs.max()) if errs.size else None,
-                             'median': float(np.median(errs)) if errs.size else None, 'n': int(errs.size)}
+                             'median': float(np.median(errs)) if errs.size else None,
+                             'within_1e-5': int((errs <= 1e-5).sum()), 'n': int(errs.size)}
+    if not a.no_laplace:
+        out['laplace_fit'] = sweep.laplace_fit()
     return out
 
 
@@ -465,6 +485,7 @@ def main():
     ap.add_argument('--sweep-n', type=int, default=64)
     ap.add_argument('--sweep-max-steps', type=int, default=100000)
     ap.add_argument('--no-plain', action='store_true')
+    ap.add_argument('--no-laplace', action='store_true', help='skip the Laplace fit of the sweep mode')
     ap.add_argument('--gpus', type=int, default=1)
     ap.add_argument('--steps', type=int, default=2000)
     ap.add_argument('--warmup', type=int, default=5)

@@ -121,4 +121,62 @@ __global__ void __launch_bounds__(BATCH_THREADS) k_batch_moments(const float *__
     batch_block_reduce(v, partials + ((size_t)blockIdx.y * gridDim.x + blockIdx.x) * BATCH_NV);
 }
 
+// Exact mass of every active lattice, rho0 V + sum of its stored populations
+// (FP64 sums of the FP32 values; slot 2 of the partials).  The density that
+// k_batch_moments sums is an FP32 sum per cell, whose rounding would bias a
+// mass correction.
+template <class L>
+__global__ void __launch_bounds__(BATCH_THREADS) k_batch_mass(const float *__restrict__ pop,
+                                                             const BatchInst *__restrict__ inst, const int Vtot,
+                                                             double *partials) {
+    const BatchInst I = inst[blockIdx.y];
+    double v[BATCH_NV] = {0.0, 0.0, 0.0};
+    if (I.active) {
+        const int V = I.Lx * I.Ly * I.Lz;
+        for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < V; g += gridDim.x * blockDim.x) {
+            double s = (double)I.rho0;
+#pragma unroll
+            for (int q = 0; q < L::Q; q++) s += (double)pop[q * Vtot + I.base + g];
+            v[2] += s;
+        }
+    }
+    batch_block_reduce(v, partials + ((size_t)blockIdx.y * gridDim.x + blockIdx.x) * BATCH_NV);
+}
+
+// add delta[i] to the rest population (q = 0) of every cell of active lattice i
+template <class L>
+__global__ void __launch_bounds__(BATCH_THREADS) k_batch_add_rest(float *__restrict__ pop,
+                                                                 const BatchInst *__restrict__ inst,
+                                                                 const float *__restrict__ delta) {
+    const BatchInst I = inst[blockIdx.y];
+    const float dl = delta[blockIdx.y];
+    if (!I.active || dl == 0.f) return;
+    const int V = I.Lx * I.Ly * I.Lz;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < V; g += gridDim.x * blockDim.x) pop[I.base + g] += dl;
+}
+
+// density (FP64 sum) at the centre cell (L_d / 2 in every dimension) and at
+// the last cell of each active lattice: the two values DeltaPLaplace reads
+// (K_NInNOut, idpy/LBM/LBMKernels.py:506-523).  One warp per lattice.
+template <class L>
+__global__ void __launch_bounds__(32) k_batch_probe(const float *__restrict__ pop, const BatchInst *__restrict__ inst,
+                                                   const int Vtot, double *out) {
+    const BatchInst I = inst[blockIdx.x];
+    if (!I.active) return;
+    const int V = I.Lx * I.Ly * I.Lz;
+    const int c = I.Lx / 2 + I.Lx * (I.Ly / 2 + I.Ly * (L::D == 3 ? I.Lz / 2 : 0));
+    const int q = threadIdx.x;
+    double a = q < L::Q ? (double)pop[q * Vtot + I.base + c] : 0.0;
+    double b = q < L::Q ? (double)pop[q * Vtot + I.base + V - 1] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    if (q == 0) {
+        out[2 * blockIdx.x] = (double)I.rho0 + a;
+        out[2 * blockIdx.x + 1] = (double)I.rho0 + b;
+    }
+}
+
 }  // namespace sclbm

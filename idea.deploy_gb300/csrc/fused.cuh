@@ -257,7 +257,10 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
                 float out;
                 if (MRT) collide_cell<L, S, true, float, false>(f, d, n, u, F, q, p, out);
                 else out = bgk_fp32<L, S>(f, u, F, q, p, C0, a, b);
-                rest_pop -= out;
+                // __fsub_rn: no contraction with the product that made `out`
+                // (at omega = 1 it is a plain multiply), so the rest population
+                // balances exactly the rounded values that are stored
+                rest_pop = __fsub_rn(rest_pop, out);
                 const int dst = X3[L::xi(q, 0) + 1] + Y3[L::xi(q, 1) + 1] + Z3[L::xi(q, D - 1) + 1];
                 pop_out[dst + q * V] = out;
             }

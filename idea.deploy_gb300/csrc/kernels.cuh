@@ -359,7 +359,7 @@ __global__ void __launch_bounds__(128) k_fcs(const Real *__restrict__ pop, Real 
             // FP32 storage: rest population from mass conservation (as the single-pass kernel)
             Real rest = d;
 #pragma unroll
-            for (int q = 1; q < Q; q++) rest -= out[q];
+            for (int q = 1; q < Q; q++) rest = __fsub_rn(rest, out[q]);  // never contracted
             out[0] = rest;
         }
 #pragma unroll

@@ -58,6 +58,13 @@ struct KernelOps {
                                  int Vtot, int gx, cudaStream_t st);
     cudaError_t (*batch_moments)(const void *pop, const void *dn, const void *psi, void *u_old, const void *sp,
                                  const BatchInst *inst, int n_inst, int Vtot, double *partials, int gx, cudaStream_t st);
+    // exact per-lattice mass, rest-population correction, centre/last-cell density
+    cudaError_t (*batch_mass)(const void *pop, const BatchInst *inst, int n_inst, int Vtot, double *partials, int gx,
+                              cudaStream_t st);
+    cudaError_t (*batch_add_rest)(void *pop, const BatchInst *inst, int n_inst, const float *delta, int gx,
+                                  cudaStream_t st);
+    cudaError_t (*batch_probe)(const void *pop, const BatchInst *inst, int n_inst, int Vtot, double *out,
+                               cudaStream_t st);
 };
 
 template <class L, class S, bool MRT, class Real, bool STRICT>
@@ -206,6 +213,30 @@ struct Ops {
         }
         return cudaErrorNotSupported;
     }
+    static cudaError_t batch_mass(const void *pop, const BatchInst *inst, int n_inst, int Vtot, double *partials,
+                                  int gx, cudaStream_t st) {
+        if constexpr (std::is_same<Real, float>::value) {
+            k_batch_mass<L><<<dim3(gx, n_inst), BATCH_THREADS, 0, st>>>((const float *)pop, inst, Vtot, partials);
+            return cudaGetLastError();
+        }
+        return cudaErrorNotSupported;
+    }
+    static cudaError_t batch_add_rest(void *pop, const BatchInst *inst, int n_inst, const float *delta, int gx,
+                                      cudaStream_t st) {
+        if constexpr (std::is_same<Real, float>::value) {
+            k_batch_add_rest<L><<<dim3(gx, n_inst), BATCH_THREADS, 0, st>>>((float *)pop, inst, delta);
+            return cudaGetLastError();
+        }
+        return cudaErrorNotSupported;
+    }
+    static cudaError_t batch_probe(const void *pop, const BatchInst *inst, int n_inst, int Vtot, double *out,
+                                   cudaStream_t st) {
+        if constexpr (std::is_same<Real, float>::value) {
+            k_batch_probe<L><<<n_inst, 32, 0, st>>>((const float *)pop, inst, Vtot, out);
+            return cudaGetLastError();
+        }
+        return cudaErrorNotSupported;
+    }
     static const KernelOps *ops() {
         constexpr bool f32 = std::is_same<Real, float>::value;
         using SH = FusedShape<L, S>;
@@ -214,7 +245,8 @@ struct Ops {
                                     f32 ? &fused : nullptr, SH::TX, SH::TY, SH::R,
                                     f32 ? &fused_occupancy : nullptr,
                                     f32 ? &batch_step : nullptr, f32 ? &batch_density : nullptr,
-                                    f32 ? &batch_moments : nullptr};
+                                    f32 ? &batch_moments : nullptr, f32 ? &batch_mass : nullptr,
+                                    f32 ? &batch_add_rest : nullptr, f32 ? &batch_probe : nullptr};
         return &o;
     }
 };

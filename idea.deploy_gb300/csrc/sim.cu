@@ -98,6 +98,13 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce_pop(const Real *__restri
     block_reduce<NV>(v, op, out);
 }
 
+// add delta to the rest population (q = 0) of every cell
+template <class Real>
+__global__ void __launch_bounds__(RED_THREADS) k_add_rest(Real *__restrict__ pop0, int64_t V, Real delta) {
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < V; g += (int64_t)gridDim.x * blockDim.x)
+        pop0[g] += delta;
+}
+
 // CheckUConvergenceSCMP: sum_d |u - u_old| summed, max |u|^2; then u_old = u
 template <class Real>
 __global__ void __launch_bounds__(RED_THREADS) k_check_u(const Real *__restrict__ u, Real *__restrict__ u_old,
@@ -1019,6 +1026,26 @@ int sclbm_density_at(sclbm_sim *s, const int64_t *idx, int count, double *out) {
     return SCLBM_OK;
 }
 
+int sclbm_restore_mass(sclbm_sim *s, double target, double *before) {
+    double m = 0;
+    int rc = sclbm_reductions(s, &m, nullptr);
+    if (rc) return rc;
+    if (before) *before = m;
+    if (!std::isfinite(target) || !std::isfinite(m)) return SCLBM_OK;
+    DevGuard dg(s->device);
+    const double delta = (target - m) / (double)s->V;
+    if (s->fp32) {
+        if ((float)delta == 0.f) return SCLBM_OK;
+        k_add_rest<float><<<s->red_blocks, RED_THREADS, 0, s->st>>>((float *)s->pop[s->cur], s->V, (float)delta);
+    } else {
+        if (delta == 0.0) return SCLBM_OK;
+        k_add_rest<double><<<s->red_blocks, RED_THREADS, 0, s->st>>>((double *)s->pop[s->cur], s->V, delta);
+    }
+    CUDA_TRY(cudaGetLastError());
+    s->moments_fresh = s->dn_fresh = false;
+    return SCLBM_OK;
+}
+
 int sclbm_density_finite(sclbm_sim *s, int *finite, double *max_abs) {
     if (!s) return fail(SCLBM_ERR_ARG, "null handle");
     DevGuard dg(s->device);
@@ -1067,6 +1094,8 @@ struct sclbm_batch {
     int cur = 0;
     void *dn = nullptr, *psi = nullptr, *u_old = nullptr;
     double *partials = nullptr;
+    double *probe_d = nullptr;  // [2n] centre / last-cell densities
+    float *delta_d = nullptr;   // [n] rest-population corrections
     int gx = 1, grid = 1;
     std::vector<int> home;  // buffer holding a retired lattice's state (-1 while active)
     std::vector<int64_t> steps;
@@ -1095,7 +1124,8 @@ void brelease(sclbm_batch *b) {
     for (auto &g : b->graph)
         if (g) cudaGraphExecDestroy(g), g = nullptr;
     for (void *p : {b->pop[0], b->pop[1], b->dn, b->psi, b->u_old, (void *)b->partials, (void *)b->inst_d,
-                    (void *)b->items_d, (void *)b->counter, (void *)b->wq_d})
+                    (void *)b->items_d, (void *)b->counter, (void *)b->wq_d, (void *)b->probe_d,
+                    (void *)b->delta_d})
         if (p) cudaFree(p);
     if (b->st) cudaStreamDestroy(b->st);
 }
@@ -1265,6 +1295,8 @@ int sclbm_batch_create(const sclbm_params *p, int n, const int *sizes, const dou
     if (!rc) rc = balloc(b, (void **)&b->items_d, sizeof(int4) * b->items.size());
     if (!rc) rc = balloc(b, (void **)&b->counter, 2 * sizeof(int));
     if (!rc) rc = balloc(b, (void **)&b->wq_d, sizeof(float) * b->Q);
+    if (!rc) rc = balloc(b, (void **)&b->probe_d, sizeof(double) * 2 * n);
+    if (!rc) rc = balloc(b, (void **)&b->delta_d, sizeof(float) * n);
     if (!rc) {
         std::vector<float> wq(b->w.begin(), b->w.end());
         if (cudaMemcpy(b->inst_d, b->inst.data(), sizeof(BatchInst) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
@@ -1433,6 +1465,52 @@ int sclbm_batch_get_density(sclbm_batch *b, int i, double *n) {
         CUDA_TRY(cudaMemcpy(tmp.data(), (const float *)b->pop[buf] + (int64_t)q * b->Vtot + b->inst[i].base,
                             V * sizeof(float), cudaMemcpyDeviceToHost));
         for (int64_t g = 0; g < V; g++) n[g] += (double)tmp[g];
+    }
+    return SCLBM_OK;
+}
+
+int sclbm_batch_restore_mass(sclbm_batch *b, const double *target, double *before) {
+    if (!b || !target) return fail(SCLBM_ERR_ARG, "bad argument");
+    if (!b->pop_set) return fail(SCLBM_ERR_STATE, "populations are not initialized");
+    DevGuard dg(b->device);
+    cudaError_t e = b->ops->batch_mass(b->pop[b->cur], b->inst_d, b->n, (int)b->Vtot, b->partials, b->gx, b->st);
+    if (e != cudaSuccess) return fail(SCLBM_ERR_CUDA, "batch mass: %s", cudaGetErrorString(e));
+    std::vector<double> part((size_t)b->n * b->gx * BATCH_NV);
+    CUDA_TRY(cudaMemcpyAsync(part.data(), b->partials, part.size() * sizeof(double), cudaMemcpyDeviceToHost, b->st));
+    CUDA_TRY(cudaStreamSynchronize(b->st));
+    std::vector<float> delta(b->n, 0.f);
+    bool any = false;
+    for (int i = 0; i < b->n; i++) {
+        if (b->home[i] >= 0) continue;  // retired
+        double m = 0;
+        for (int k = 0; k < b->gx; k++) m += part[((size_t)i * b->gx + k) * BATCH_NV + 2];
+        if (before) before[i] = m;
+        if (std::isfinite(target[i]) && std::isfinite(m)) {
+            delta[i] = (float)((target[i] - m) / (double)lattice_cells(b, i));
+            any = any || delta[i] != 0.f;
+        }
+    }
+    if (!any) return SCLBM_OK;
+    CUDA_TRY(cudaMemcpyAsync(b->delta_d, delta.data(), sizeof(float) * b->n, cudaMemcpyHostToDevice, b->st));
+    e = b->ops->batch_add_rest(b->pop[b->cur], b->inst_d, b->n, b->delta_d, b->gx, b->st);
+    if (e != cudaSuccess) return fail(SCLBM_ERR_CUDA, "batch mass correction: %s", cudaGetErrorString(e));
+    CUDA_TRY(cudaStreamSynchronize(b->st));
+    return SCLBM_OK;
+}
+
+int sclbm_batch_probe(sclbm_batch *b, double *n_in, double *n_out) {
+    if (!b) return fail(SCLBM_ERR_ARG, "null handle");
+    if (!b->pop_set) return fail(SCLBM_ERR_STATE, "populations are not initialized");
+    DevGuard dg(b->device);
+    cudaError_t e = b->ops->batch_probe(b->pop[b->cur], b->inst_d, b->n, (int)b->Vtot, b->probe_d, b->st);
+    if (e != cudaSuccess) return fail(SCLBM_ERR_CUDA, "batch probe: %s", cudaGetErrorString(e));
+    std::vector<double> v((size_t)2 * b->n);
+    CUDA_TRY(cudaMemcpyAsync(v.data(), b->probe_d, v.size() * sizeof(double), cudaMemcpyDeviceToHost, b->st));
+    CUDA_TRY(cudaStreamSynchronize(b->st));
+    for (int i = 0; i < b->n; i++) {
+        if (b->home[i] >= 0) continue;  // retired: keep the caller's last values
+        if (n_in) n_in[i] = v[2 * i];
+        if (n_out) n_out[i] = v[2 * i + 1];
     }
     return SCLBM_OK;
 }

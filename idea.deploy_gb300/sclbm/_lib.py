@@ -92,6 +92,9 @@ SIGNATURES = {
     'sclbm_batch_check': [_P, _P, _P, _P],
     'sclbm_batch_set_active': [_P, _P],
     'sclbm_batch_steps': [_P, _P],
+    'sclbm_batch_restore_mass': [_P, _P, _P],
+    'sclbm_batch_probe': [_P, _P, _P],
+    'sclbm_restore_mass': [_P, _D, _DP],
     'sclbm_step_noalloc': [ctypes.POINTER(Params), _P, _P, _P],
 }
 _STR = {'sclbm_version', 'sclbm_status_string', 'sclbm_last_error'}
@@ -302,6 +305,12 @@ class Sim:
         out = np.empty(idx.size)
         call('sclbm_density_at', self.h, idx.ctypes.data_as(_I64P), int(idx.size), dptr(out))
         return out
+
+    def restore_mass(self, target=float('nan')):
+        """FP64 mass before; if target is finite, restore it (rest populations)."""
+        m = ctypes.c_double()
+        call('sclbm_restore_mass', self.h, float(target), ctypes.byref(m))
+        return m.value
 
     def density_finite(self):
         f, m = ctypes.c_int(), ctypes.c_double()

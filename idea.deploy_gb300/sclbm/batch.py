@@ -101,6 +101,19 @@ class Batch:
         _lib.call('sclbm_batch_check', self.h, _lib.ptr(uc), _lib.ptr(mu), _lib.ptr(m))
         return uc, mu, m
 
+    def restore_mass(self, target=None):
+        """Per-lattice FP64 mass before; where target is finite, restore it."""
+        t = np.full(self.n, np.nan) if target is None else np.ascontiguousarray(np.asarray(target, np.float64))
+        before = np.full(self.n, np.nan)
+        _lib.call('sclbm_batch_restore_mass', self.h, _lib.ptr(t), _lib.ptr(before))
+        return before
+
+    def probe(self):
+        """Per-lattice density at the centre cell and at the last cell."""
+        a, b = np.full(self.n, np.nan), np.full(self.n, np.nan)
+        _lib.call('sclbm_batch_probe', self.h, _lib.ptr(a), _lib.ptr(b))
+        return a, b
+
     def set_active(self, active):
         self.active = np.ascontiguousarray(np.asarray(active, np.int32))
         _lib.call('sclbm_batch_set_active', self.h, _lib.ptr(self.active))

@@ -1,21 +1,31 @@
 """Droplet sweeps: coexistence densities, batched FP32 droplets, FP64 plain runs.
 
-* ``coexistence(G, ...)``: the plain method (FP64 GPU path) on a flat
-  interface (a periodic slab, the reference's ``InitFlatInterface``,
-  idpy/LBM/MultiPhase.py:1855-1895), stepped until the velocity stops
-  changing; returns the bulk liquid and gas densities.
+* ``coexistence_many(Gs, ...)``: the plain method (FP64 GPU path) on flat
+  interfaces (periodic slabs, the reference's ``InitFlatInterface``,
+  idpy/LBM/MultiPhase.py:1855-1895), one handle and stream per coupling, all
+  stepped together.  With psi = exp(-1/n) well below the critical coupling
+  (G_c = -e^2/3 = -2.46) the slabs do not settle: they keep breathing
+  (max|u| ~ 1e-2 .. 1e-1 for 10^6 steps, on the CPU oracle as on the GPU), so
+  the bulk densities are averaged over the second half of the run and their
+  spread is reported; the slabs that blow up are reported as diverged.  The
+  thermodynamic coexistence (``sclbm.thermo``, the reference's SCThermo) is
+  the starting guess and the comparison.
 * ``ragged_sweep(...)``: droplets of radius R in boxes of side 4R rounded up
-  to a multiple of 32, couplings G, densities from ``coexistence``; all run in
-  one ``Batch`` (FP32-shifted storage, FP64 reductions) and are retired one by
-  one as they converge.
-* ``plain_runs(...)``: the same droplets one after another on the plain FP64
-  GPU path, for the error and time-to-converge comparison.
+  to a multiple of 32, couplings G, all in one ``Batch`` (FP32-shifted storage
+  shifted by the gas density, FP64 reductions), retired one by one as they
+  converge.  At every check the FP64 mass of each lattice is restored (FP32
+  rounding repeats in a near-steady state and would drift the mass
+  linearly).
+* ``plain_run(...)``: the same droplet on the plain FP64 GPU path.
 
-Convergence is the reference's measure (CheckUConvergenceSCMP,
-idpy/LBM/MultiPhaseLoopChecks.py:96-163): u_conv = sum_cells sum_d
-|u(t) - u(t-K)| / V between two checks K steps apart, against a threshold.
-A Shan-Chen droplet keeps steady spurious currents, so max|u| itself never
-falls to zero; its value at convergence is reported.
+Convergence.  A Shan-Chen droplet keeps steady spurious currents (max|u| of
+0.1 .. 0.3 here), so max|u| never falls to 1e-9; the criteria are the
+reference's: the FP64 run stops when u_conv = sum|u(t) - u(t-K)| / V < 1e-12
+(CheckUConvergenceSCMP, idpy/LBM/MultiPhaseLoopChecks.py:96-163, FP64
+threshold); the FP32 batch stops when the Laplace pressure changes by less
+than ``tol_dp`` (relative) between ``patience`` consecutive checks
+(CheckCenterOfMassDeltaPConvergence, MultiPhaseLoopChecks.py:35-91, whose
+threshold is 1e-5), and reports the mean of those last values.
 """
 import math
 import time
@@ -25,6 +35,7 @@ import numpy as np
 from . import _lib
 from .LBM import XIStencils, FStencils
 from .profiles import droplet
+from . import thermo
 
 
 def psi_exp(n):
@@ -44,96 +55,131 @@ def slab(L, n_l, n_g, width=4.0, rows=4):
     return np.tile(prof, (rows, 1))
 
 
-def coexistence(G, stencil='D2E8', tau=1.0, L=128, width=4.0, guess=None, check_every=1000,
-                max_steps=200000, tol=1e-12, device=0):
-    """Bulk (rho_l, rho_g) of a flat interface at coupling G (FP64 plain path).
+def thermo_guess(G, stencil='D2E8'):
+    """(rho_l, rho_g) of the thermodynamic flat-interface construction, or None."""
+    f = FStencils[stencil]
+    try:
+        t = thermo.coexistence(G, f['Es'], f['Ws'])
+        return t['n_l'], t['n_g']
+    except (ValueError, RuntimeError):
+        return None
 
-    Returns dict(rho_l, rho_g, steps, u_conv, finite)."""
+
+def coexistence_many(Gs, stencil='D2E8', L=128, rows=4, steps=200000, sample_every=2000, tol=1e-11,
+                     width=4.0, device=0):
+    """Flat-interface (slab) runs for many couplings at once on the FP64 plain
+    path.  Returns per G: rho_l, rho_g (final values if the slab settled, else
+    means over the second half), their spread, max|u| at the end, status
+    'steady' / 'breathing' / 'diverged', and the thermodynamic values."""
     x, f = XIStencils['D2Q9'], FStencils[stencil]
-    if guess is None:
-        # a start in the two-phase region: the coexisting densities grow ~linearly with -G
-        guess = (max(0.25, 4.6 + 1.4 * (-4.5 - G)), 0.2)
-    n_l, n_g = guess
-    dims = (L, 4)
-    s = _lib.Sim(2, dims, x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], G, tau=tau, literals=_lib.LIT_EXACT,
-                 device=device)
-    s.set_density(slab(L, n_l, n_g, width))
-    s.set_velocity(np.zeros(2 * s.V))
-    s.init_populations()
-    steps, uc, finite = 0, float('nan'), True
-    s.compute_moments()
-    s.check_u()
-    while steps < max_steps:
-        s.step(check_every)
-        steps += check_every
+    sims, out = [], []
+    for G in Gs:
+        th = thermo_guess(G, stencil)
+        nl0, ng0 = th if th else (max(0.25, 4.6 + 1.4 * (-4.5 - G)), 0.2)
+        s = _lib.Sim(2, (L, rows), x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], G, literals=_lib.LIT_EXACT,
+                     device=device)
+        s.set_density(slab(L, nl0, ng0, width, rows))
+        s.set_velocity(np.zeros(2 * s.V))
+        s.init_populations()
+        sims.append(s)
+        out.append(dict(G=float(G), thermo_rho_l=th[0] if th else None, thermo_rho_g=th[1] if th else None,
+                        samples=[]))
+    probe = [L // 2, 0]
+    for k in range(steps // sample_every):
+        for s in sims:
+            s.step(sample_every, sync=False)
+        if 2 * (k + 1) * sample_every > steps:
+            for i, s in enumerate(sims):
+                out[i]['samples'].append(s.density_at(probe))
+    for i, s in enumerate(sims):
+        smp = np.array(out[i].pop('samples'))
         s.compute_moments()
-        uc, _ = s.check_u()
-        finite = s.density_finite()[0]
-        if not finite or not np.isfinite(uc) or uc < tol:
-            break
-    n = s.get_density().reshape(4, L)
-    s.close()
-    return dict(rho_l=float(n[0, L // 2]), rho_g=float(n[0, 0]), steps=steps, u_conv=float(uc),
-                finite=bool(finite and np.isfinite(n).all()))
+        s.check_u()
+        s.step(sample_every)
+        s.compute_moments()
+        uc, mu = s.check_u()
+        fin = np.isfinite(smp).all() and np.isfinite(uc) and s.density_finite()[0]
+        o = out[i]
+        o.update(steps=steps, u_conv=float(uc), max_u=float(mu))
+        if not fin:
+            o.update(status='diverged', rho_l=float('nan'), rho_g=float('nan'))
+        elif uc < tol:
+            n = s.density_at(probe)
+            o.update(status='steady', rho_l=float(n[0]), rho_g=float(n[1]), rho_l_spread=0.0, rho_g_spread=0.0)
+        else:
+            o.update(status='breathing', rho_l=float(smp[:, 0].mean()), rho_g=float(smp[:, 1].mean()),
+                     rho_l_spread=float(smp[:, 0].std()), rho_g_spread=float(smp[:, 1].std()))
+        s.close()
+    return out
 
 
 def sweep_geometry(radii, multiple=32, factor=4):
     return [int(math.ceil(factor * R / multiple) * multiple) for R in radii]
 
 
-def ragged_sweep(radii, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, check_every=500, tol=1e-7,
-                 max_steps=200000, noise=0.0, seed=0, device=0, init=None):
+def ragged_sweep(radii, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, check_every=500, tol_dp=2e-5,
+                 patience=4, max_steps=200000, noise=0.0, seed=0, device=0, init=None, mass_fix=True):
     """Run all droplets in one FP32 batch until each converges; returns a dict
     of per-droplet arrays and the wall time.  ``init`` may give initial
     density fields (e.g. a learned warm start) instead of the tanh profile."""
     boxes = sweep_geometry(radii)
     sizes = [(L, L) for L in boxes]
-    rho0 = [0.5 * (a + b) for a, b in zip(rho_l, rho_g)]
+    n = len(radii)
     t0 = time.perf_counter()
-    b = Batch_(XIStencils['D2Q9'], FStencils[stencil], sizes, G, rho0, tau=tau, device=device)
+    # the shift is the gas density: most cells are gas, whose small
+    # populations then keep most of their FP32 digits
+    b = Batch_(XIStencils['D2Q9'], FStencils[stencil], sizes, G, list(rho_g), tau=tau, device=device)
     for i, (R, L) in enumerate(zip(radii, boxes)):
         n0 = init[i] if init is not None else droplet((L, L), R, rho_l[i], rho_g[i], width, seed + i, noise)
         b.set_density(i, n0)
     b.init_populations()
-    n = len(radii)
+    m0 = b.restore_mass()
     active = np.ones(n, np.int32)
-    steps_done = np.zeros(n, np.int64)
-    u_conv = np.full(n, np.nan)
-    max_u = np.full(n, np.nan)
+    u_conv, max_u = np.full(n, np.nan), np.full(n, np.nan)
     status = np.array(['running'] * n, dtype=object)
+    hist = [[] for _ in range(n)]
+    calm = np.zeros(n, np.int64)
+    n_in, n_out = np.full(n, np.nan), np.full(n, np.nan)
     b.check()  # u_old := u of the initial state
     total = 0
     while active.any() and total < max_steps:
         b.step(check_every, sync=False)
         total += check_every
-        uc, mu, m = b.check()
+        uc, mu, _ = b.check()
+        if mass_fix:
+            b.restore_mass(m0)
+        ni, no = b.probe()
         for i in np.nonzero(active)[0]:
             u_conv[i], max_u[i] = uc[i], mu[i]
-            if not (np.isfinite(uc[i]) and np.isfinite(m[i])):
+            n_in[i], n_out[i] = ni[i], no[i]
+            dp = laplace_dp(ni[i], no[i], G[i])[0]
+            if not (np.isfinite(uc[i]) and np.isfinite(dp)):
                 status[i], active[i] = 'diverged', 0
-            elif uc[i] < tol:
+                continue
+            if hist[i] and abs(dp - hist[i][-1]) <= tol_dp * abs(dp):
+                calm[i] += 1
+            else:
+                calm[i] = 0
+            hist[i].append(dp)
+            if calm[i] >= patience:
                 status[i], active[i] = 'converged', 0
-        steps_done[:] = b.steps()
         if not active.all():
             b.set_active(active)
+    steps = b.steps()
     wall = time.perf_counter() - t0
-    dp, n_in, n_out = [], [], []
-    for i, L in enumerate(boxes):
-        nf = b.get_density(i)
-        ni, no = nf[L // 2, L // 2], nf[L - 1, L - 1]
-        n_in.append(ni)
-        n_out.append(no)
-        dp.append(laplace_dp(ni, no, G[i])[0])
     b.close()
     status[status == 'running'] = 'max_steps'
-    return dict(radii=np.array(radii), boxes=np.array(boxes), G=np.array(G), steps=steps_done, u_conv=u_conv,
-                max_u=max_u, status=status, dp=np.array(dp), n_in=np.array(n_in), n_out=np.array(n_out),
-                wall_s=wall)
+    dp = np.array([np.mean(h[-patience:]) if h else np.nan for h in hist])
+    return dict(radii=np.array(radii), boxes=np.array(boxes), G=np.array(G), steps=steps, u_conv=u_conv,
+                max_u=max_u, status=status, dp=dp, n_in=n_in, n_out=n_out, wall_s=wall)
 
 
-def plain_run(R, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, check_every=500, tol=1e-7,
-              max_steps=200000, noise=0.0, seed=0, device=0):
-    """One droplet on the plain FP64 GPU path (exact coefficients), same criterion."""
+def plain_run(R, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, check_every=500, tol=1e-12,
+              max_steps=200000, noise=0.0, seed=0, device=0, tol_dp=2e-5, patience=4):
+    """One droplet on the plain FP64 GPU path (exact coefficients), stopped by
+    the reference's FP64 criterion u_conv < tol.  The step and wall time at
+    which the FP32 batch's criterion (Laplace pressure calm to tol_dp for
+    `patience` checks) would first have stopped it are recorded too."""
     L = sweep_geometry([R])[0]
     x, f = XIStencils['D2Q9'], FStencils[stencil]
     t0 = time.perf_counter()
@@ -144,7 +190,9 @@ def plain_run(R, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, check_ever
     s.init_populations()
     s.compute_moments()
     s.check_u()
-    steps, uc, status = 0, float('nan'), 'max_steps'
+    steps, uc, mu, status = 0, float('nan'), float('nan'), 'max_steps'
+    probe = [(L // 2) * L + L // 2, L * L - 1]
+    prev, calm, steps_dp, wall_dp = None, 0, None, None
     while steps < max_steps:
         s.step(check_every)
         steps += check_every
@@ -153,84 +201,85 @@ def plain_run(R, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, check_ever
         if not np.isfinite(uc) or not s.density_finite()[0]:
             status = 'diverged'
             break
+        if steps_dp is None:
+            ni, no = s.density_at(probe)
+            dp = laplace_dp(ni, no, G)[0]
+            calm = calm + 1 if prev is not None and abs(dp - prev) <= tol_dp * abs(dp) else 0
+            prev = dp
+            if calm >= patience:
+                steps_dp, wall_dp = steps, time.perf_counter() - t0
         if uc < tol:
             status = 'converged'
             break
-    nf = s.get_density().reshape(L, L)
+    ni, no = s.density_at(probe)
     s.close()
-    ni, no = nf[L // 2, L // 2], nf[L - 1, L - 1]
-    return dict(R=R, L=L, steps=steps, u_conv=uc, status=status, dp=laplace_dp(ni, no, G)[0], n_in=ni, n_out=no,
-                wall_s=time.perf_counter() - t0)
+    return dict(R=R, L=L, steps=steps, u_conv=uc, max_u=mu, status=status, dp=laplace_dp(ni, no, G)[0], n_in=ni,
+                n_out=no, wall_s=time.perf_counter() - t0, steps_dp=steps_dp, wall_dp_s=wall_dp)
 
 
-def coexistence_many(Gs, stencil='D2E8', check_every=2000, max_steps=200000, tol=1e-11, L=128, device=0):
-    """``coexistence`` for many couplings at once: every slab has its own
-    handle and stream, so their (launch-bound) steps overlap on the GPU."""
-    x, f = XIStencils['D2Q9'], FStencils[stencil]
-    sims, out = [], []
-    for G in Gs:
-        s = _lib.Sim(2, (L, 4), x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], G, literals=_lib.LIT_EXACT,
-                     device=device)
-        s.set_density(slab(L, max(0.25, 4.6 + 1.4 * (-4.5 - G)), 0.2))
-        s.set_velocity(np.zeros(2 * s.V))
-        s.init_populations()
-        s.compute_moments()
-        s.check_u()
-        sims.append(s)
-        out.append(dict(G=float(G), steps=0, u_conv=float('nan'), status='running'))
-    running = list(range(len(Gs)))
-    while running:
-        for i in running:
-            sims[i].step(check_every, sync=False)
-        for i in list(running):
-            s = sims[i]
-            s.compute_moments()
-            uc, _ = s.check_u()
-            out[i]['steps'] += check_every
-            out[i]['u_conv'] = uc
-            if not np.isfinite(uc) or not s.density_finite()[0]:
-                out[i]['status'] = 'diverged'
-            elif uc < tol:
-                out[i]['status'] = 'converged'
-            elif out[i]['steps'] >= max_steps:
-                out[i]['status'] = 'max_steps'
-            if out[i]['status'] != 'running':
-                running.remove(i)
-    for i, s in enumerate(sims):
-        n = s.get_density().reshape(4, L)
-        out[i]['rho_l'], out[i]['rho_g'] = float(n[0, L // 2]), float(n[0, 0])
-        s.close()
-    return out
+def laplace_fit(G=-4.5, radii=(12, 16, 20, 24, 32, 40, 48), stencil='D2E8', device=0, **kw):
+    """Laplace test at one coupling: the FP32 batch at several radii, then
+    dP = sigma / R + c fitted by least squares (2D Laplace law); returns
+    sigma, c, the per-droplet values and the thermodynamic sigma_f."""
+    f = FStencils[stencil]
+    th = thermo.coexistence(G, f['Es'], f['Ws'])
+    radii = list(radii)
+    r = ragged_sweep(radii, [G] * len(radii), [th['n_l']] * len(radii), [th['n_g']] * len(radii),
+                     stencil=stencil, device=device, **kw)
+    ok = r['status'] == 'converged'
+    A = np.stack([1.0 / r['radii'][ok], np.ones(ok.sum())], 1)
+    (sigma, c), *_ = np.linalg.lstsq(A, r['dp'][ok], rcond=None)
+    return dict(G=G, sigma=float(sigma), intercept=float(c), sigma_thermo=th['sigma_f'],
+                radii=[int(v) for v in r['radii']], dp=[float(v) for v in r['dp']],
+                status=[str(v) for v in r['status']], steps=[int(v) for v in r['steps']])
 
 
-def run_sweep(n=64, r_min=8, seed=2024, G_range=(-6.0, -4.5), stencil='D2E8', check_every=500, tol32=1e-5,
-              tol64=1e-9, max_steps=100000, plain=True, device=0, init=None):
+def run_sweep(n=64, r_min=8, seed=2024, G_range=(-6.0, -4.5), stencil='D2E8', check_every=500, tol_dp=2e-5,
+              tol64=1e-12, max_steps=100000, coex_steps=200000, plain=True, device=0, init=None):
     """The ragged droplet sweep: radii r_min .. r_min+n-1, box 4R rounded up to
-    32, G uniform in G_range (seeded), densities from the coexistence runs;
-    batched FP32 run vs the plain FP64 path droplet by droplet."""
+    32, G uniform in G_range (seeded), densities from the flat-interface runs
+    (from the thermodynamic construction where the slab diverged); batched
+    FP32 run vs the plain FP64 path droplet by droplet."""
     rng = np.random.default_rng(seed)
     radii = list(range(r_min, r_min + n))
     Gs = rng.uniform(G_range[0], G_range[1], n)
     t0 = time.perf_counter()
-    coex = coexistence_many(Gs, stencil=stencil, device=device)
+    coex = coexistence_many(Gs, stencil=stencil, steps=coex_steps, device=device)
     t_coex = time.perf_counter() - t0
-    ok = [i for i, c in enumerate(coex) if c['status'] != 'diverged' and np.isfinite(c['rho_l'])]
-    unstable = [dict(R=radii[i], G=float(Gs[i]), reason='flat interface diverged') for i in range(n) if i not in ok]
-    rl = [coex[i]['rho_l'] for i in ok]
-    rg = [coex[i]['rho_g'] for i in ok]
-    sw = ragged_sweep([radii[i] for i in ok], [float(Gs[i]) for i in ok], rl, rg, stencil=stencil,
-                      check_every=check_every, tol=tol32, max_steps=max_steps, device=device,
-                      init=None if init is None else [init[i] for i in ok])
+    rl, rg, source = [], [], []
+    for c in coex:
+        ok = c['status'] != 'diverged'
+        rl.append(c['rho_l'] if ok else c['thermo_rho_l'])
+        rg.append(c['rho_g'] if ok else c['thermo_rho_g'])
+        source.append('flat interface (%s)' % c['status'] if ok else 'thermodynamics')
+    sw = ragged_sweep(radii, [float(g) for g in Gs], rl, rg, stencil=stencil, check_every=check_every,
+                      tol_dp=tol_dp, max_steps=max_steps, device=device, init=init)
+    unstable = []
+    for i in range(n):
+        why = []
+        if coex[i]['status'] == 'diverged':
+            why.append('flat interface diverged (droplet densities from thermodynamics)')
+        if sw['status'][i] == 'diverged':
+            why.append('droplet diverged after %d steps (FP32 batch)' % sw['steps'][i])
+        if why:
+            unstable.append(dict(R=radii[i], G=float(Gs[i]), reason='; '.join(why)))
     res = dict(config=dict(n=n, radii=[r_min, r_min + n - 1], box='4R rounded up to 32', G_range=list(G_range),
-                           seed=seed, stencil=stencil, tau=1.0, check_every=check_every, tol_fp32=tol32,
-                           tol_fp64=tol64, criterion='u_conv = sum|u(t)-u(t-K)|/V (CheckUConvergenceSCMP)'),
-               coexistence_wall_s=t_coex, unstable=unstable, batch=sw,
-               coexistence=[coex[i] for i in ok])
+                           seed=seed, stencil=stencil, tau=1.0, check_every=check_every, tol_dp_fp32=tol_dp,
+                           patience=4, tol_u_fp64=tol64, coexistence_steps=coex_steps,
+                           fp32_shift='rho_g per droplet', fp32_mass='restored to the initial FP64 mass at each check',
+                           criterion_fp32='relative change of the Laplace pressure between checks '
+                                          '(CheckCenterOfMassDeltaPConvergence)',
+                           criterion_fp64='u_conv = sum|u(t)-u(t-K)|/V < tol (CheckUConvergenceSCMP)'),
+               coexistence_wall_s=t_coex, unstable=unstable, batch=sw, coexistence=coex, rho_l=rl, rho_g=rg,
+               rho_source=source)
     if plain:
         runs = []
         t1 = time.perf_counter()
-        for j, i in enumerate(ok):
-            runs.append(plain_run(radii[i], float(Gs[i]), rl[j], rg[j], stencil=stencil, check_every=check_every,
+        for i in range(n):
+            if sw['status'][i] == 'diverged':
+                runs.append(None)
+                continue
+            runs.append(plain_run(radii[i], float(Gs[i]), rl[i], rg[i], stencil=stencil, check_every=check_every,
                                   tol=tol64, max_steps=max_steps, device=device))
         res['plain'] = runs
         res['plain_wall_s'] = time.perf_counter() - t1

@@ -185,6 +185,14 @@ SCLBM_API int sclbm_center_of_mass(sclbm_sim *s, double *mass, double *cm);
 SCLBM_API int sclbm_density_at(sclbm_sim *s, const int64_t *idx, int count, double *out);
 /* 1 if every density value is finite, else 0 (max |n| also returned) */
 SCLBM_API int sclbm_density_finite(sclbm_sim *s, int *finite, double *max_abs);
+/* Mass restoring: *before = the FP64 mass of the current populations; if
+ * target is finite, (target - mass) / V is then added to the rest population
+ * of every cell.  FP32-shifted storage rounds every stored population, and in
+ * a near-steady state the same rounding repeats every step, so the mass drifts
+ * linearly (about 1e-9 relative per step); a caller that checks convergence
+ * every K steps restores the initial mass there.  No counterpart in the
+ * reference, whose FP64 step conserves mass to round-off. */
+SCLBM_API int sclbm_restore_mass(sclbm_sim *s, double target, double *before);
 
 /* ---------------------------------------------------------------------------
  * Batches: many independent periodic lattices of different sizes (ragged
@@ -221,6 +229,15 @@ SCLBM_API int sclbm_batch_check(sclbm_batch *b, double *u_conv, double *max_u, d
 SCLBM_API int sclbm_batch_set_active(sclbm_batch *b, const int *active);
 /* steps each lattice has taken */
 SCLBM_API int sclbm_batch_steps(const sclbm_batch *b, int64_t *steps);
+/* sclbm_restore_mass per active lattice: before[i] = its FP64 mass; where
+ * target[i] is finite, (target[i] - mass) / V_i is added to its rest
+ * populations. */
+SCLBM_API int sclbm_batch_restore_mass(sclbm_batch *b, const double *target, double *before);
+/* density (FP64 sum of the populations) at the centre cell (L_d / 2 in every
+ * dimension) and at the last cell of every active lattice: the two densities
+ * of DeltaPLaplace (idpy/LBM/MultiPhase.py:1690-1757, K_NInNOut
+ * idpy/LBM/LBMKernels.py:506-523).  Retired lattices keep their last values. */
+SCLBM_API int sclbm_batch_probe(sclbm_batch *b, double *n_in, double *n_out);
 
 /* ---------------------------------------------------------------------------
  * One step that allocates no device memory.  No counterpart in the reference.

@@ -91,3 +91,63 @@ def test_batch_rejects_bad_input():
         Batch(XIStencils[lat], FStencils[st], [(64, 1)], [-4.5], [1.0])
     with pytest.raises(_lib.SclbmError):
         Batch(XIStencils[lat], FStencils['D3E6'], [(64, 64)], [-4.5], [1.0])
+
+
+def test_batch_probe_reads_centre_and_last_cell():
+    lat, st, dims, G, rho0 = CASES['2d']
+    n0 = densities(dims)
+    b = Batch(XIStencils[lat], FStencils[st], dims, G, rho0)
+    for i, n in enumerate(n0):
+        b.set_density(i, n)
+    b.init_populations()
+    b.step(17)
+    ni, no = b.probe()
+    for i, d in enumerate(dims):
+        nf = b.get_density(i)
+        assert abs(ni[i] - nf[d[1] // 2, d[0] // 2]) < 1e-12 * abs(ni[i])
+        assert abs(no[i] - nf[-1, -1]) < 1e-12 * abs(no[i])
+    # retired lattices keep the caller's values
+    b.set_active([1, 0, 1])
+    a, c = np.full(3, -1.0), np.full(3, -1.0)
+    _lib.call('sclbm_batch_probe', b.h, _lib.ptr(a), _lib.ptr(c))
+    assert a[1] == -1.0 and c[1] == -1.0 and a[0] != -1.0
+    b.close()
+
+
+def test_batch_restore_mass_sets_each_lattice_mass():
+    lat, st, dims, G, rho0 = CASES['2d']
+    n0 = densities(dims)
+    b = Batch(XIStencils[lat], FStencils[st], dims, G, [0.2, 0.2, 0.2])
+    for i, n in enumerate(n0):
+        b.set_density(i, n)
+    b.init_populations()
+    m0 = b.restore_mass()
+    for i, n in enumerate(n0):
+        assert abs(m0[i] / n.sum() - 1) < 1e-6   # FP32 storage of the initial field
+    b.step(300)
+    m1 = b.restore_mass()
+    target = m1 * (1 + np.array([1e-5, 0.0, -2e-5]))
+    target[1] = np.nan                           # lattice 1: no correction
+    b.restore_mass(target)
+    m2 = b.restore_mass()
+    assert abs(m2[0] / target[0] - 1) < 1e-7 and abs(m2[2] / target[2] - 1) < 1e-7
+    assert m2[1] == m1[1]
+    b.close()
+
+
+def test_restore_mass_single_handle():
+    x, f = XIStencils['D2Q9'], FStencils['D2E8']
+    dims = (96, 80)
+    s = _lib.Sim(2, dims, x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], -4.6, precision=_lib.FP32_SHIFTED,
+                 rho0=0.2)
+    s.set_density(droplet(dims, 20, 4.7, 0.2, 2.0, 5))
+    s.set_velocity(np.zeros(2 * s.V))
+    s.init_populations()
+    m0 = s.restore_mass()
+    s.step(500)
+    s.restore_mass(m0 * (1 + 3e-5))
+    m1 = s.restore_mass()
+    assert abs(m1 / (m0 * (1 + 3e-5)) - 1) < 1e-7
+    m2, _ = s.reductions()
+    assert m2 == m1
+    s.close()
