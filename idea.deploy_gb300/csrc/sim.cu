@@ -32,6 +32,20 @@ int fail(int code, const char *fmt, ...) {
     return code;
 }
 
+}  // namespace
+
+namespace sclbm {
+// the last-error message of this thread, for the other translation units of
+// the library (sclbm_last_error reads it)
+int set_error(int code, const char *msg) {
+    g_err = msg ? msg : "";
+    return code;
+}
+void clear_error() { g_err.clear(); }
+}  // namespace sclbm
+
+namespace {
+
 #define CUDA_TRY(call)                                                                                \
     do {                                                                                              \
         cudaError_t e_ = (call);                                                                      \

@@ -95,6 +95,15 @@ SIGNATURES = {
     'sclbm_batch_restore_mass': [_P, _P, _P],
     'sclbm_batch_probe': [_P, _P, _P],
     'sclbm_restore_mass': [_P, _D, _DP],
+    'sclbm_mlp_param_count': [_IP],
+    'sclbm_mlp_create': [ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(_P)],
+    'sclbm_mlp_destroy': [_P],
+    'sclbm_mlp_set_params': [_P, _P],
+    'sclbm_mlp_get_params': [_P, _P],
+    'sclbm_mlp_set_data': [_P, _I64, _P, _P],
+    'sclbm_mlp_train': [_P, _I64, _I64, ctypes.c_float, _P],
+    'sclbm_mlp_gradient': [_P, _I64, _P, _P, _P, _P],
+    'sclbm_mlp_predict': [_P, _I64, _P, _P],
     'sclbm_step_noalloc': [ctypes.POINTER(Params), _P, _P, _P],
 }
 _STR = {'sclbm_version', 'sclbm_status_string', 'sclbm_last_error'}

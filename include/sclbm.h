@@ -240,6 +240,36 @@ SCLBM_API int sclbm_batch_restore_mass(sclbm_batch *b, const double *target, dou
 SCLBM_API int sclbm_batch_probe(sclbm_batch *b, double *n_in, double *n_out);
 
 /* ---------------------------------------------------------------------------
+ * Warm-start surrogate: an MLP 5 -> 64 -> 64 -> 64 -> 1 with SiLU, BF16
+ * parameters (FP32 master copy) and FP32 accumulation, trained with Adam on
+ * (input, target) pairs the caller gives (normalised features of a droplet
+ * and a radial position -> normalised density).  No counterpart in the
+ * reference, which starts every droplet from a tanh profile.  Parameters are
+ * one float vector of sclbm_mlp_param_count() values:
+ * W1[64][5], b1[64], W2[64][64], b2[64], W3[64][64], b3[64], W4[64], b4.
+ * ------------------------------------------------------------------------- */
+typedef struct sclbm_mlp sclbm_mlp;
+SCLBM_API int sclbm_mlp_param_count(int *count);
+/* weights and biases uniform in +-1/sqrt(fan_in) from the seed */
+SCLBM_API int sclbm_mlp_create(int device, uint64_t seed, sclbm_mlp **out);
+SCLBM_API int sclbm_mlp_destroy(sclbm_mlp *m);
+/* FP32 master parameters; setting them also resets the Adam state and step */
+SCLBM_API int sclbm_mlp_set_params(sclbm_mlp *m, const float *w);
+SCLBM_API int sclbm_mlp_get_params(sclbm_mlp *m, float *w);
+/* training set: n inputs x[n][5] and targets t[n] (copied to the device) */
+SCLBM_API int sclbm_mlp_set_data(sclbm_mlp *m, int64_t n, const float *x, const float *t);
+/* steps of Adam (beta 0.9 / 0.999, eps 1e-8) on the mean squared error of
+ * `batch` samples drawn on the device per step; loss[steps] (optional) gets
+ * the loss of every step */
+SCLBM_API int sclbm_mlp_train(sclbm_mlp *m, int64_t steps, int64_t batch, float lr, float *loss);
+/* gradient of the mean squared error over the n given samples with the
+ * current parameters (no update): grad[param_count], *loss */
+SCLBM_API int sclbm_mlp_gradient(sclbm_mlp *m, int64_t n, const float *x, const float *t, float *grad,
+                                 float *loss);
+/* outputs y[n] for inputs x[n][5] */
+SCLBM_API int sclbm_mlp_predict(sclbm_mlp *m, int64_t n, const float *x, float *y);
+
+/* ---------------------------------------------------------------------------
  * One step that allocates no device memory.  No counterpart in the reference.
  *
  * For callers that cannot let this library call cudaMalloc: a host program
