@@ -479,6 +479,60 @@ def run_sweep_mode(a):
     return out
 
 
+def batch_vs_plain(bres, plain):
+    """Status counts, wall time and Laplace-pressure error of a batched run
+    against the plain FP64 runs of the same droplets."""
+    out = {'wall_s': round(bres['wall_s'], 3),
+           'status': {str(k): int((bres['status'] == k).sum()) for k in set(bres['status'])},
+           'steps_mean': float(np.mean(bres['steps'])), 'steps_max': int(np.max(bres['steps']))}
+    if bres.get('fallback') is not None and np.isfinite(bres['residual']).any():
+        res = bres['residual'][np.isfinite(bres['residual'])]
+        out['warm_residual'] = {'median': float(np.median(res)), 'max': float(res.max())}
+        out['cold_fallbacks'] = int(bres['fallback'].sum())
+    if plain is not None:
+        errs = np.array([abs(bres['dp'][j] - p['dp']) / max(abs(p['dp']), 1e-300) for j, p in enumerate(plain)
+                         if p is not None and p['status'] == 'converged' and bres['status'][j] == 'converged'])
+        out['dp_rel_err_vs_fp64'] = {'median': float(np.median(errs)) if errs.size else None,
+                                     'max': float(errs.max()) if errs.size else None,
+                                     'within_1e-5': int((errs <= 1e-5).sum()), 'n': int(errs.size)}
+    return out
+
+
+def run_warmstart_mode(a):
+    """Learned warm start: plain-method equilibrium profiles, MLP training on
+    the device, held-out evaluation, then the droplet sweep started cold and
+    warm against the plain FP64 path."""
+    from sclbm import sweep, warmstart
+    t0 = time.perf_counter()
+    prof, st = warmstart.equilibrium_profiles(n=a.ws_profiles, max_steps=a.ws_max_steps)
+    train_set, test_set = warmstart.split(prof, holdout=512)
+    m, loss, wall_train = warmstart.train(train_set, steps=a.ws_train_steps, batch=8192, lr=1e-3)
+    ev = warmstart.evaluate(m, test_set)
+    r = sweep.run_sweep(n=a.sweep_n, max_steps=a.sweep_max_steps, plain=not a.no_plain, mlp=m)
+    plain = r.get('plain')
+    out = {'metric': 'D2Q9 E8 droplet sweep with a learned warm start: time to converge', 'unit': 's',
+           'profiles': {'requested': a.ws_profiles, 'status': st['status'], 'wall_s': round(st['wall_s'], 2),
+                        'train': len(train_set), 'held_out': len(test_set),
+                        'method': 'FP32 batched LBM to the Laplace-pressure criterion, radial bins of 0.5'},
+           'training': {'steps': a.ws_train_steps, 'batch': 8192, 'lr': 1e-3, 'wall_s': round(wall_train, 3),
+                        'loss_first': float(loss[:10].mean()), 'loss_last': float(loss[-100:].mean()),
+                        'samples': int(sum(len(p['r']) for p in train_set))},
+           'held_out': ev,
+           'sweep': {'config': r['config'], 'coexistence_wall_s': round(r['coexistence_wall_s'], 2),
+                     'unstable': len(r['unstable']),
+                     'batch_cold': batch_vs_plain(r['batch'], plain),
+                     'batch_warm': batch_vs_plain(r['warm'], plain)}}
+    if plain is not None:
+        out['sweep']['plain_fp64'] = {'wall_s': round(r['plain_wall_s'], 3),
+                                      'status': {k: sum(1 for p in plain if p is not None and p['status'] == k)
+                                                 for k in ('converged', 'max_steps', 'diverged')}}
+        out['speedup_wall_cold'] = round(r['plain_wall_s'] / r['batch']['wall_s'], 2)
+        out['speedup_wall_warm'] = round(r['plain_wall_s'] / r['warm']['wall_s'], 2)
+    out['total_wall_s'] = round(time.perf_counter() - t0, 1)
+    m.close()
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--sweep', action='store_true', help='run the ragged droplet sweep instead')
@@ -486,6 +540,10 @@ def main():
     ap.add_argument('--sweep-max-steps', type=int, default=100000)
     ap.add_argument('--no-plain', action='store_true')
     ap.add_argument('--no-laplace', action='store_true', help='skip the Laplace fit of the sweep mode')
+    ap.add_argument('--warmstart', action='store_true', help='learned warm start: profiles, training, sweep')
+    ap.add_argument('--ws-profiles', type=int, default=4096)
+    ap.add_argument('--ws-max-steps', type=int, default=60000)
+    ap.add_argument('--ws-train-steps', type=int, default=20000)
     ap.add_argument('--gpus', type=int, default=1)
     ap.add_argument('--steps', type=int, default=2000)
     ap.add_argument('--warmup', type=int, default=5)
@@ -501,6 +559,9 @@ def main():
         BOX = (a.box, a.box, a.box)
     if a.sweep:
         print(json.dumps(run_sweep_mode(a)))
+        return 0
+    if a.warmstart:
+        print(json.dumps(run_warmstart_mode(a)))
         return 0
     if a.impl == 'reference':
         ws, rank, _ = dist_env()

@@ -1355,6 +1355,7 @@ int sclbm_batch_info(const sclbm_batch *b, int64_t *cells, int64_t *device_bytes
 int sclbm_batch_set_density(sclbm_batch *b, int i, const double *n) {
     if (!b || !n || i < 0 || i >= b->n) return fail(SCLBM_ERR_ARG, "bad argument");
     DevGuard dg(b->device);
+    CUDA_TRY(cudaStreamSynchronize(b->st));  // the observables kernels use dn as scratch
     const int64_t V = lattice_cells(b, i);
     std::vector<float> tmp(V);
     for (int64_t g = 0; g < V; g++) tmp[g] = (float)(n[g] - (double)b->inst[i].rho0);
@@ -1375,6 +1376,23 @@ int sclbm_batch_init_populations(sclbm_batch *b) {
     CUDA_TRY(cudaGetLastError());
     CUDA_TRY(cudaStreamSynchronize(b->st));
     b->pop_set = true;
+    return SCLBM_OK;
+}
+
+int sclbm_batch_init_lattice(sclbm_batch *b, int i) {
+    if (!b || i < 0 || i >= b->n) return fail(SCLBM_ERR_ARG, "bad argument");
+    if (!b->pop_set) return fail(SCLBM_ERR_STATE, "call sclbm_batch_init_populations first");
+    if (b->home[i] >= 0) return fail(SCLBM_ERR_STATE, "lattice %d is retired", i);
+    DevGuard dg(b->device);
+    const dim3 grid(b->gx, 1);
+    if (b->D == 2)
+        k_batch_init<D2Q9><<<grid, BATCH_THREADS, 0, b->st>>>((float *)b->pop[b->cur], (const float *)b->dn,
+                                                             b->inst_d + i, (int)b->Vtot, b->wq_d);
+    else
+        k_batch_init<D3Q19><<<grid, BATCH_THREADS, 0, b->st>>>((float *)b->pop[b->cur], (const float *)b->dn,
+                                                              b->inst_d + i, (int)b->Vtot, b->wq_d);
+    CUDA_TRY(cudaGetLastError());
+    CUDA_TRY(cudaStreamSynchronize(b->st));
     return SCLBM_OK;
 }
 

@@ -93,6 +93,7 @@ SIGNATURES = {
     'sclbm_batch_set_active': [_P, _P],
     'sclbm_batch_steps': [_P, _P],
     'sclbm_batch_restore_mass': [_P, _P, _P],
+    'sclbm_batch_init_lattice': [_P, ctypes.c_int],
     'sclbm_batch_probe': [_P, _P, _P],
     'sclbm_restore_mass': [_P, _D, _DP],
     'sclbm_mlp_param_count': [_IP],

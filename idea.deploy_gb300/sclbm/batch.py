@@ -80,6 +80,10 @@ class Batch:
     def init_populations(self):
         _lib.call('sclbm_batch_init_populations', self.h)
 
+    def init_lattice(self, i):
+        """Equilibrium populations of lattice i alone from its last set density."""
+        _lib.call('sclbm_batch_init_lattice', self.h, int(i))
+
     def step(self, nsteps, sync=True):
         _lib.call('sclbm_batch_step', self.h, int(nsteps))
         if sync:

@@ -118,21 +118,41 @@ def sweep_geometry(radii, multiple=32, factor=4):
 
 
 def ragged_sweep(radii, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, check_every=500, tol_dp=2e-5,
-                 patience=4, max_steps=200000, noise=0.0, seed=0, device=0, init=None, mass_fix=True):
+                 patience=4, max_steps=200000, noise=0.0, seed=0, device=0, init=None, mass_fix=True,
+                 residual_steps=100, residual_max=None, return_fields=False):
     """Run all droplets in one FP32 batch until each converges; returns a dict
     of per-droplet arrays and the wall time.  ``init`` may give initial
-    density fields (e.g. a learned warm start) instead of the tanh profile."""
+    density fields (e.g. a learned warm start) instead of the tanh profile,
+    shifted by a constant to the tanh start's mass; with ``residual_max``
+    every such start is first stepped ``residual_steps`` steps, and a lattice
+    whose density changed by more than residual_max (relative L2 norm of the
+    change against the spread of the start) is restarted from the tanh
+    profile (cold-start fallback)."""
     boxes = sweep_geometry(radii)
     sizes = [(L, L) for L in boxes]
     n = len(radii)
     t0 = time.perf_counter()
+    cold = lambda i: droplet((boxes[i], boxes[i]), radii[i], rho_l[i], rho_g[i], width, seed + i, noise)
+    if init is not None:
+        # a given start carries the mass of the tanh start, so both reach the same equilibrium
+        init = [np.asarray(f, np.float64) + (cold(i).sum() - np.sum(f)) / np.size(f) for i, f in enumerate(init)]
     # the shift is the gas density: most cells are gas, whose small
     # populations then keep most of their FP32 digits
     b = Batch_(XIStencils['D2Q9'], FStencils[stencil], sizes, G, list(rho_g), tau=tau, device=device)
-    for i, (R, L) in enumerate(zip(radii, boxes)):
-        n0 = init[i] if init is not None else droplet((L, L), R, rho_l[i], rho_g[i], width, seed + i, noise)
-        b.set_density(i, n0)
+    for i in range(n):
+        b.set_density(i, init[i] if init is not None else cold(i))
     b.init_populations()
+    residual = np.full(n, np.nan)
+    fallback = np.zeros(n, bool)
+    if init is not None and residual_max is not None:
+        b.step(residual_steps)
+        for i in range(n):
+            d = b.get_density(i) - init[i]
+            residual[i] = np.linalg.norm(d) / max(np.linalg.norm(init[i] - init[i].mean()), 1e-300)
+            if not (residual[i] <= residual_max):
+                fallback[i] = True
+                b.set_density(i, cold(i))
+                b.init_lattice(i)
     m0 = b.restore_mass()
     active = np.ones(n, np.int32)
     u_conv, max_u = np.full(n, np.nan), np.full(n, np.nan)
@@ -167,11 +187,13 @@ def ragged_sweep(radii, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, che
             b.set_active(active)
     steps = b.steps()
     wall = time.perf_counter() - t0
+    fields = [b.get_density(i) for i in range(n)] if return_fields else None
     b.close()
     status[status == 'running'] = 'max_steps'
     dp = np.array([np.mean(h[-patience:]) if h else np.nan for h in hist])
     return dict(radii=np.array(radii), boxes=np.array(boxes), G=np.array(G), steps=steps, u_conv=u_conv,
-                max_u=max_u, status=status, dp=dp, n_in=n_in, n_out=n_out, wall_s=wall)
+                max_u=max_u, status=status, dp=dp, n_in=n_in, n_out=n_out, wall_s=wall, residual=residual,
+                fallback=fallback, fields=fields)
 
 
 def plain_run(R, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, check_every=500, tol=1e-12,
@@ -235,7 +257,8 @@ def laplace_fit(G=-4.5, radii=(12, 16, 20, 24, 32, 40, 48), stencil='D2E8', devi
 
 
 def run_sweep(n=64, r_min=8, seed=2024, G_range=(-6.0, -4.5), stencil='D2E8', check_every=500, tol_dp=2e-5,
-              tol64=1e-12, max_steps=100000, coex_steps=200000, plain=True, device=0, init=None):
+              tol64=1e-12, max_steps=100000, coex_steps=200000, plain=True, device=0, init=None, mlp=None,
+              residual_max=0.1):
     """The ragged droplet sweep: radii r_min .. r_min+n-1, box 4R rounded up to
     32, G uniform in G_range (seeded), densities from the flat-interface runs
     (from the thermodynamic construction where the slab diverged); batched
@@ -254,6 +277,21 @@ def run_sweep(n=64, r_min=8, seed=2024, G_range=(-6.0, -4.5), stencil='D2E8', ch
         source.append('flat interface (%s)' % c['status'] if ok else 'thermodynamics')
     sw = ragged_sweep(radii, [float(g) for g in Gs], rl, rg, stencil=stencil, check_every=check_every,
                       tol_dp=tol_dp, max_steps=max_steps, device=device, init=init)
+    warm = None
+    if mlp is not None:
+        # the same droplets started from the network's predicted profiles,
+        # their radii set so that each carries the mass of its tanh start
+        from .warmstart import warm_fields
+        t1 = time.perf_counter()
+        masses = [droplet((L, L), R, a, b_, 2.0, 0, 0.0).sum()
+                  for R, L, a, b_ in zip(radii, sweep_geometry(radii), rl, rg)]
+        fields = warm_fields(mlp, radii, [float(g) for g in Gs], order=int(stencil[-1]), masses=masses)
+        t_pred = time.perf_counter() - t1
+        warm = ragged_sweep(radii, [float(g) for g in Gs], rl, rg, stencil=stencil, check_every=check_every,
+                            tol_dp=tol_dp, max_steps=max_steps, device=device, init=fields,
+                            residual_max=residual_max)
+        warm['predict_wall_s'] = t_pred
+        warm['wall_s'] += t_pred
     unstable = []
     for i in range(n):
         why = []
@@ -271,7 +309,7 @@ def run_sweep(n=64, r_min=8, seed=2024, G_range=(-6.0, -4.5), stencil='D2E8', ch
                                           '(CheckCenterOfMassDeltaPConvergence)',
                            criterion_fp64='u_conv = sum|u(t)-u(t-K)|/V < tol (CheckUConvergenceSCMP)'),
                coexistence_wall_s=t_coex, unstable=unstable, batch=sw, coexistence=coex, rho_l=rl, rho_g=rg,
-               rho_source=source)
+               rho_source=source, warm=warm)
     if plain:
         runs = []
         t1 = time.perf_counter()

@@ -217,6 +217,10 @@ SCLBM_API int sclbm_batch_set_density(sclbm_batch *b, int i, const double *n);
 SCLBM_API int sclbm_batch_get_density(sclbm_batch *b, int i, double *n);
 /* equilibrium populations of every lattice from its density (u = 0) */
 SCLBM_API int sclbm_batch_init_populations(sclbm_batch *b);
+/* equilibrium populations (u = 0) of active lattice i alone from the density
+ * last given by sclbm_batch_set_density (a restart of one lattice, e.g. a
+ * warm start that is replaced by a cold start) */
+SCLBM_API int sclbm_batch_init_lattice(sclbm_batch *b, int i);
 /* enqueue nsteps steps of every active lattice (returns without waiting) */
 SCLBM_API int sclbm_batch_step(sclbm_batch *b, int64_t nsteps);
 SCLBM_API int sclbm_batch_step_timed(sclbm_batch *b, int64_t nsteps, double *ms);
