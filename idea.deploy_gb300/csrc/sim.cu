@@ -1110,7 +1110,7 @@ struct sclbm_batch {
     double *partials = nullptr;
     double *probe_d = nullptr;  // [2n] centre / last-cell densities
     float *delta_d = nullptr;   // [n] rest-population corrections
-    int gx = 1, grid = 1;
+    int gx = 1, grid = 1, chunk = 32;
     std::vector<int> home;  // buffer holding a retired lattice's state (-1 while active)
     std::vector<int64_t> steps;
     bool pop_set = false;
@@ -1120,7 +1120,8 @@ struct sclbm_batch {
 
 namespace {
 
-constexpr int BATCH_CHUNK = 32;     // planes per work item
+constexpr int BATCH_CHUNK = 32;     // longest run of planes per work item
+constexpr int BATCH_MIN_CHUNK = 4;  // shortest (items are re-planned as lattices retire)
 constexpr int BATCH_CHECK_BLOCKS = 32;  // blocks per lattice in the observable kernels
 
 int balloc(sclbm_batch *b, void **p, size_t bytes) {
@@ -1148,6 +1149,47 @@ int64_t lattice_cells(const sclbm_batch *b, int i) {
     int64_t v = 1;
     for (int d = 0; d < b->D; d++) v *= b->sizes[(size_t)i * b->D + d];
     return v;
+}
+
+// Work items of the active lattices: tiles x runs of `chunk` marching planes.
+// A work item's planes are processed one after another (each a global-memory
+// round trip and a barrier), so the step time has a floor of about
+// (chunk + 2R) plane latencies; the chunk is the longest one that still gives
+// two items per resident CTA, and no shorter than BATCH_MIN_CHUNK (each item
+// re-reads 2R halo planes).
+void batch_items(const sclbm_batch *b, int chunk, std::vector<int4> &items) {
+    items.clear();
+    const int TX = b->ops->fused_tx, TY = b->ops->fused_ty;
+    for (int i = 0; i < b->n; i++) {
+        if (!b->inst[i].active) continue;
+        const BatchInst &I = b->inst[i];
+        const int Lm = b->D == 3 ? I.Lz : I.Ly;
+        for (int m0 = 0; m0 < Lm; m0 += chunk)
+            for (int y0 = 0; y0 < (b->D == 3 ? I.Ly : 1); y0 += TY)
+                for (int x0 = 0; x0 < I.Lx; x0 += TX)
+                    items.push_back(make_int4(i, x0, y0, m0 | (std::min(m0 + chunk, Lm) << 16)));
+    }
+}
+
+int batch_plan(sclbm_batch *b) {
+    const int resident = b->sms * b->ops->fused_occupancy();
+    int chunk = BATCH_CHUNK;
+    std::vector<int4> items;
+    batch_items(b, chunk, items);
+    while (chunk > BATCH_MIN_CHUNK && (int)items.size() < 2 * resident) {
+        chunk = std::max(BATCH_MIN_CHUNK, chunk / 2);
+        batch_items(b, chunk, items);
+    }
+    for (auto &g : b->graph)
+        if (g) cudaGraphExecDestroy(g), g = nullptr;  // they hold the item count and grid
+    b->items.swap(items);
+    b->chunk = chunk;
+    if (!b->items.empty())
+        CUDA_TRY(cudaMemcpyAsync(b->items_d, b->items.data(), sizeof(int4) * b->items.size(), cudaMemcpyHostToDevice,
+                                 b->st));
+    CUDA_TRY(cudaStreamSynchronize(b->st));
+    b->grid = std::max(1, std::min((int)b->items.size(), resident));
+    return SCLBM_OK;
 }
 
 int batch_launch_step(sclbm_batch *b) {
@@ -1260,11 +1302,6 @@ int sclbm_batch_create(const sclbm_params *p, int n, const int *sizes, const dou
         I.active = 1;
         I.pad = 0;
         b->inst.push_back(I);
-        const int Lm = b->D == 3 ? I.Lz : I.Ly;
-        for (int m0 = 0; m0 < Lm; m0 += BATCH_CHUNK)
-            for (int y0 = 0; y0 < (b->D == 3 ? I.Ly : 1); y0 += TY)
-                for (int x0 = 0; x0 < I.Lx; x0 += TX)
-                    b->items.push_back(make_int4(i, x0, y0, m0 | (std::min(m0 + BATCH_CHUNK, Lm) << 16)));
         base += lattice_cells(b, i);
     }
     // step parameters (BGK, FP32); G and rho0 come from the lattice table
@@ -1306,7 +1343,11 @@ int sclbm_batch_create(const sclbm_params *p, int n, const int *sizes, const dou
     b->gx = BATCH_CHECK_BLOCKS;
     if (!rc) rc = balloc(b, (void **)&b->partials, (size_t)n * b->gx * BATCH_NV * sizeof(double));
     if (!rc) rc = balloc(b, (void **)&b->inst_d, sizeof(BatchInst) * n);
-    if (!rc) rc = balloc(b, (void **)&b->items_d, sizeof(int4) * b->items.size());
+    {
+        std::vector<int4> most;  // the longest item list: every lattice, the shortest chunk
+        batch_items(b, BATCH_MIN_CHUNK, most);
+        if (!rc) rc = balloc(b, (void **)&b->items_d, sizeof(int4) * most.size());
+    }
     if (!rc) rc = balloc(b, (void **)&b->counter, 2 * sizeof(int));
     if (!rc) rc = balloc(b, (void **)&b->wq_d, sizeof(float) * b->Q);
     if (!rc) rc = balloc(b, (void **)&b->probe_d, sizeof(double) * 2 * n);
@@ -1314,17 +1355,12 @@ int sclbm_batch_create(const sclbm_params *p, int n, const int *sizes, const dou
     if (!rc) {
         std::vector<float> wq(b->w.begin(), b->w.end());
         if (cudaMemcpy(b->inst_d, b->inst.data(), sizeof(BatchInst) * n, cudaMemcpyHostToDevice) != cudaSuccess ||
-            cudaMemcpy(b->items_d, b->items.data(), sizeof(int4) * b->items.size(), cudaMemcpyHostToDevice) !=
-                cudaSuccess ||
             cudaMemcpy(b->wq_d, wq.data(), sizeof(float) * b->Q, cudaMemcpyHostToDevice) != cudaSuccess ||
             cudaMemset(b->counter, 0, 2 * sizeof(int)) != cudaSuccess ||
             cudaMemset(b->u_old, 0, fb * b->D) != cudaSuccess || cudaMemset(b->dn, 0, fb) != cudaSuccess)
             rc = fail(SCLBM_ERR_CUDA, "batch upload: %s", cudaGetErrorString(cudaGetLastError()));
     }
-    if (!rc) {
-        const int occ = b->ops->fused_occupancy();
-        b->grid = std::max(1, std::min((int)b->items.size(), b->sms * occ));
-    }
+    if (!rc) rc = batch_plan(b);
     if (rc) {
         brelease(b);
         delete b;
@@ -1481,7 +1517,7 @@ int sclbm_batch_set_active(sclbm_batch *b, const int *active) {
     }
     CUDA_TRY(cudaMemcpyAsync(b->inst_d, b->inst.data(), sizeof(BatchInst) * b->n, cudaMemcpyHostToDevice, b->st));
     CUDA_TRY(cudaStreamSynchronize(b->st));
-    return SCLBM_OK;
+    return batch_plan(b);  // work items of the lattices still stepping
 }
 
 int sclbm_batch_get_density(sclbm_batch *b, int i, double *n) {
