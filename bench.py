@@ -533,6 +533,39 @@ def run_warmstart_mode(a):
     return out
 
 
+def run_sweep3d_mode(a):
+    """3D batched droplets (256 D3Q19 E6 droplets in 96^3 boxes, FP32 batches)
+    against the plain FP64 path on a timed sample, extrapolated."""
+    from sclbm import sweep
+    r = sweep.run_sweep3d(n=a.sweep3d_n, max_steps=a.sweep3d_max_steps, plain_sample=a.sweep3d_plain)
+    b = r['batch']
+    ok = b['status'] == 'converged'
+    out = {'metric': 'D3Q19 E6 batched droplets (96^3 boxes): time to converge, batched FP32 vs plain FP64',
+           'unit': 's', 'config': r['config'],
+           'batch': {'wall_s': round(b['wall_s'], 2), 'batches': b['batches'],
+                     'status': {str(k): int((b['status'] == k).sum()) for k in set(b['status'])},
+                     'steps_mean_converged': float(b['steps'][ok].mean()) if ok.any() else None,
+                     'cell_updates': float(sum(int(st) for st in b['steps']) * r['config']['box'] ** 3)}}
+    rows = []
+    for p in r['plain']:
+        i = p['index']
+        rows.append({'R': round(float(b['radii'][i]), 3), 'G': round(float(b['G'][i]), 4), 'steps32': int(b['steps'][i]),
+                     'steps64': int(p['steps']), 'status64': p['status'], 'wall64_s': round(p['wall_s'], 3),
+                     'steps64_dp_criterion': p['steps_dp'],
+                     'dp_rel_err': float(abs(b['dp'][i] - p['dp']) / abs(p['dp']))})
+    out['plain_sample'] = rows
+    if rows:
+        w = np.mean([x['wall64_s'] for x in rows])
+        wdp = np.mean([(p['wall_dp_s'] if p['wall_dp_s'] is not None else p['wall_s']) for p in r['plain']])
+        n_ok = int(ok.sum())
+        out['plain_extrapolated'] = {'wall_per_droplet_s': round(float(w), 3), 'droplets': n_ok,
+                                     'wall_s': round(float(w * n_ok), 1),
+                                     'wall_same_criterion_s': round(float(wdp * n_ok), 1)}
+        out['speedup_wall_estimate'] = round(float(w * n_ok / b['wall_s']), 2)
+        out['speedup_wall_same_criterion_estimate'] = round(float(wdp * n_ok / b['wall_s']), 2)
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--sweep', action='store_true', help='run the ragged droplet sweep instead')
@@ -541,6 +574,10 @@ def main():
     ap.add_argument('--no-plain', action='store_true')
     ap.add_argument('--no-laplace', action='store_true', help='skip the Laplace fit of the sweep mode')
     ap.add_argument('--warmstart', action='store_true', help='learned warm start: profiles, training, sweep')
+    ap.add_argument('--sweep3d', action='store_true', help='3D batched droplets vs plain FP64 (sampled)')
+    ap.add_argument('--sweep3d-n', type=int, default=256)
+    ap.add_argument('--sweep3d-max-steps', type=int, default=20000)
+    ap.add_argument('--sweep3d-plain', type=int, default=8)
     ap.add_argument('--ws-profiles', type=int, default=4096)
     ap.add_argument('--ws-max-steps', type=int, default=60000)
     ap.add_argument('--ws-train-steps', type=int, default=20000)
@@ -562,6 +599,9 @@ def main():
         return 0
     if a.warmstart:
         print(json.dumps(run_warmstart_mode(a)))
+        return 0
+    if a.sweep3d:
+        print(json.dumps(run_sweep3d_mode(a)))
         return 0
     if a.impl == 'reference':
         ws, rank, _ = dist_env()

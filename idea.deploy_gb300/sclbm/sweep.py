@@ -119,7 +119,7 @@ def sweep_geometry(radii, multiple=32, factor=4):
 
 def ragged_sweep(radii, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, check_every=500, tol_dp=2e-5,
                  patience=4, max_steps=200000, noise=0.0, seed=0, device=0, init=None, mass_fix=True,
-                 residual_steps=100, residual_max=None, return_fields=False):
+                 residual_steps=100, residual_max=None, return_fields=False, dim=2, boxes=None):
     """Run all droplets in one FP32 batch until each converges; returns a dict
     of per-droplet arrays and the wall time.  ``init`` may give initial
     density fields (e.g. a learned warm start) instead of the tanh profile,
@@ -128,17 +128,18 @@ def ragged_sweep(radii, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, che
     whose density changed by more than residual_max (relative L2 norm of the
     change against the spread of the start) is restarted from the tanh
     profile (cold-start fallback)."""
-    boxes = sweep_geometry(radii)
-    sizes = [(L, L) for L in boxes]
+    boxes = list(boxes) if boxes is not None else sweep_geometry(radii)
+    sizes = [(L,) * dim for L in boxes]
     n = len(radii)
     t0 = time.perf_counter()
-    cold = lambda i: droplet((boxes[i], boxes[i]), radii[i], rho_l[i], rho_g[i], width, seed + i, noise)
+    cold = lambda i: droplet(sizes[i], radii[i], rho_l[i], rho_g[i], width, seed + i, noise)
     if init is not None:
         # a given start carries the mass of the tanh start, so both reach the same equilibrium
         init = [np.asarray(f, np.float64) + (cold(i).sum() - np.sum(f)) / np.size(f) for i, f in enumerate(init)]
     # the shift is the gas density: most cells are gas, whose small
     # populations then keep most of their FP32 digits
-    b = Batch_(XIStencils['D2Q9'], FStencils[stencil], sizes, G, list(rho_g), tau=tau, device=device)
+    b = Batch_(XIStencils['D2Q9' if dim == 2 else 'D3Q19'], FStencils[stencil], sizes, G, list(rho_g), tau=tau,
+               device=device)
     for i in range(n):
         b.set_density(i, init[i] if init is not None else cold(i))
     b.init_populations()
@@ -197,23 +198,25 @@ def ragged_sweep(radii, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, che
 
 
 def plain_run(R, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, check_every=500, tol=1e-12,
-              max_steps=200000, noise=0.0, seed=0, device=0, tol_dp=2e-5, patience=4):
+              max_steps=200000, noise=0.0, seed=0, device=0, tol_dp=2e-5, patience=4, dim=2, L=None):
     """One droplet on the plain FP64 GPU path (exact coefficients), stopped by
     the reference's FP64 criterion u_conv < tol.  The step and wall time at
     which the FP32 batch's criterion (Laplace pressure calm to tol_dp for
     `patience` checks) would first have stopped it are recorded too."""
-    L = sweep_geometry([R])[0]
-    x, f = XIStencils['D2Q9'], FStencils[stencil]
+    L = L or sweep_geometry([R])[0]
+    dims = (L,) * dim
+    x, f = XIStencils['D2Q9' if dim == 2 else 'D3Q19'], FStencils[stencil]
     t0 = time.perf_counter()
-    s = _lib.Sim(2, (L, L), x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], G, tau=tau, literals=_lib.LIT_EXACT,
+    s = _lib.Sim(dim, dims, x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], G, tau=tau, literals=_lib.LIT_EXACT,
                  device=device)
-    s.set_density(droplet((L, L), R, rho_l, rho_g, width, seed, noise))
-    s.set_velocity(np.zeros(2 * s.V))
+    s.set_density(droplet(dims, R, rho_l, rho_g, width, seed, noise))
+    s.set_velocity(np.zeros(dim * s.V))
     s.init_populations()
     s.compute_moments()
     s.check_u()
     steps, uc, mu, status = 0, float('nan'), float('nan'), 'max_steps'
-    probe = [(L // 2) * L + L // 2, L * L - 1]
+    c = L // 2
+    probe = [c + L * c + (L * L * c if dim == 3 else 0), s.V - 1]
     prev, calm, steps_dp, wall_dp = None, 0, None, None
     while steps < max_steps:
         s.step(check_every)
@@ -322,6 +325,47 @@ def run_sweep(n=64, r_min=8, seed=2024, G_range=(-6.0, -4.5), stencil='D2E8', ch
         res['plain'] = runs
         res['plain_wall_s'] = time.perf_counter() - t1
     return res
+
+
+def run_sweep3d(n=256, seed=2025, R_range=(10.0, 30.0), G_range=(-6.0, -4.5), L=96, stencil='D3E6', check_every=500,
+                tol_dp=2e-5, tol64=1e-12, max_steps=20000, plain_sample=8, device=0):
+    """Batched 3D droplets: n D3Q19 droplets, radius and G uniform in their
+    ranges (seeded), each in an L^3 periodic box, FP32-shifted batches (split
+    so that Q * cells < 2^31 per batch); then the plain FP64 path, cold
+    started, on `plain_sample` of the droplets the batch converged, timed one
+    after another.  Start densities: the flat-interface thermodynamic
+    construction of the 2D stencil of the same order (sclbm.thermo has the 2D
+    pressure-tensor constants)."""
+    rng = np.random.default_rng(seed)
+    radii = rng.uniform(*R_range, n)
+    Gs = rng.uniform(*G_range, n)
+    guess = [thermo_guess(g, 'D2E' + stencil[-1]) or (4.6, 0.2) for g in Gs]
+    rl = [a for a, _ in guess]
+    rg = [b for _, b in guess]
+    per = max(1, ((1 << 31) - 1) // (19 * L ** 3) - 1)
+    groups = np.array_split(np.arange(n), int(math.ceil(n / per)))
+    t0 = time.perf_counter()
+    parts = []
+    for gi in groups:
+        parts.append(ragged_sweep([float(radii[i]) for i in gi], [float(Gs[i]) for i in gi], [rl[i] for i in gi],
+                                  [rg[i] for i in gi], stencil=stencil, check_every=check_every, tol_dp=tol_dp,
+                                  max_steps=max_steps, device=device, dim=3, boxes=[L] * len(gi), seed=seed))
+    wall = time.perf_counter() - t0
+    cat = lambda k: np.concatenate([p[k] for p in parts])
+    batch = dict(radii=radii, G=Gs, steps=cat('steps'), status=cat('status'), dp=cat('dp'), max_u=cat('max_u'),
+                 wall_s=wall, batches=[len(g) for g in groups])
+    ok = np.nonzero(batch['status'] == 'converged')[0]
+    pick = rng.choice(ok, size=min(plain_sample, len(ok)), replace=False) if len(ok) else []
+    plain = []
+    for i in pick:
+        r = plain_run(float(radii[i]), float(Gs[i]), rl[i], rg[i], stencil=stencil, check_every=check_every,
+                      tol=tol64, max_steps=max_steps, device=device, dim=3, L=L, seed=seed + int(i))
+        r['index'] = int(i)
+        plain.append(r)
+    return dict(config=dict(n=n, seed=seed, R_range=list(R_range), G_range=list(G_range), box=L, stencil=stencil,
+                            tau=1.0, check_every=check_every, tol_dp_fp32=tol_dp, tol_u_fp64=tol64,
+                            max_steps=max_steps, plain_sample=len(plain)),
+                batch=batch, plain=plain, rho_l=rl, rho_g=rg)
 
 
 # late import (batch imports MultiPhase, which imports this package's _lib)

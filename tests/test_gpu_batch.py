@@ -151,3 +151,16 @@ def test_restore_mass_single_handle():
     m2, _ = s.reductions()
     assert m2 == m1
     s.close()
+
+
+def test_3d_droplets_batch_matches_plain_fp64():
+    from sclbm import sweep
+    radii, G = [6.0, 8.0], [-4.6, -4.7]
+    guess = [sweep.thermo_guess(g, 'D2E6') for g in G]
+    rl, rg = [a for a, _ in guess], [b for _, b in guess]
+    b = sweep.ragged_sweep(radii, G, rl, rg, stencil='D3E6', dim=3, boxes=[32, 32], max_steps=30000)
+    assert (b['status'] == 'converged').all(), b['status']
+    for i in range(2):
+        p = sweep.plain_run(radii[i], G[i], rl[i], rg[i], stencil='D3E6', dim=3, L=32, max_steps=60000, tol=1e-11)
+        assert p['status'] == 'converged'
+        assert abs(b['dp'][i] / p['dp'] - 1) < 1e-3, (b['dp'][i], p['dp'])
