@@ -191,7 +191,9 @@ def ragged_sweep(radii, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, che
     fields = [b.get_density(i) for i in range(n)] if return_fields else None
     b.close()
     status[status == 'running'] = 'max_steps'
-    dp = np.array([np.mean(h[-patience:]) if h else np.nan for h in hist])
+    # converged: the mean of the calm checks; otherwise the last value
+    dp = np.array([(np.mean(h[-patience:]) if st == 'converged' else h[-1]) if h else np.nan
+                   for h, st in zip(hist, status)])
     return dict(radii=np.array(radii), boxes=np.array(boxes), G=np.array(G), steps=steps, u_conv=u_conv,
                 max_u=max_u, status=status, dp=dp, n_in=n_in, n_out=n_out, wall_s=wall, residual=residual,
                 fallback=fallback, fields=fields)

@@ -158,9 +158,11 @@ def test_3d_droplets_batch_matches_plain_fp64():
     radii, G = [6.0, 8.0], [-4.6, -4.7]
     guess = [sweep.thermo_guess(g, 'D2E6') for g in G]
     rl, rg = [a for a, _ in guess], [b for _, b in guess]
-    b = sweep.ragged_sweep(radii, G, rl, rg, stencil='D3E6', dim=3, boxes=[32, 32], max_steps=30000)
-    assert (b['status'] == 'converged').all(), b['status']
+    # both paths run the same 6000 steps (no early stop), then the Laplace
+    # pressures of the FP32 batch and the FP64 plain path are compared
+    b = sweep.ragged_sweep(radii, G, rl, rg, stencil='D3E6', dim=3, boxes=[32, 32], max_steps=6000, tol_dp=0.0)
+    assert (b['status'] == 'max_steps').all() and (b['steps'] == 6000).all(), (b['status'], b['steps'])
     for i in range(2):
-        p = sweep.plain_run(radii[i], G[i], rl[i], rg[i], stencil='D3E6', dim=3, L=32, max_steps=60000, tol=1e-11)
-        assert p['status'] == 'converged'
-        assert abs(b['dp'][i] / p['dp'] - 1) < 1e-3, (b['dp'][i], p['dp'])
+        p = sweep.plain_run(radii[i], G[i], rl[i], rg[i], stencil='D3E6', dim=3, L=32, max_steps=6000, tol=0.0)
+        assert p['steps'] == 6000 and p['status'] == 'max_steps'
+        assert abs(b["dp"][i] / p["dp"] - 1) < 2e-4, (b["dp"][i], p["dp"])
