@@ -269,8 +269,10 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
     }
 }
 
+// Three CTAs per SM for BGK (80 registers, no spills; 5% faster than two at
+// 256^3 D3Q19 E6, measured in one run), two for the dense MRT operator.
 template <class L, class S, bool MRT>
-__global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
+__global__ void __launch_bounds__(FusedShape<L, S>::NT, MRT ? 2 : 3)
     k_fused(const float *__restrict__ pop, float *__restrict__ pop_out, const __grid_constant__ StepParams<L, S, float> p,
             const FusedGeom fg) {
     using SH = FusedShape<L, S>;
