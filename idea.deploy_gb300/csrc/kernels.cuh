@@ -371,6 +371,90 @@ __global__ void __launch_bounds__(128) k_fcs(const Real *__restrict__ pop, Real 
 }
 
 // ---------------------------------------------------------------------------
+// walls (GetWalls / MainLoopWalls, idpy/LBM/MultiPhase.py:157-162,1226-1309):
+// walls[g] = 1 fluid, 0 wall.  Density and psi on fluid cells only (walls keep
+// the psi they were given, K_ComputeDensityPsiWallsMeta,
+// MultiPhaseKernelsMeta.py:42-105); the step on fluid cells only, a population
+// whose push target is a wall going to the opposite population of its own cell
+// (halfway bounce-back, Collisions.py:705-860).  Wall cells carry their
+// populations unchanged from buffer to buffer (the reference leaves them
+// stale), so the total mass stays constant.
+// ---------------------------------------------------------------------------
+template <class L>
+SCLBM_HD constexpr int opposite_q(int q) {
+    for (int k = 0; k < L::Q; k++) {
+        bool same = true;
+        for (int d = 0; d < L::D; d++) same = same && (L::xi(k, d) == -L::xi(q, d));
+        if (same) return k;
+    }
+    return q;
+}
+
+template <class L, class Real>
+__global__ void __launch_bounds__(256) k_density_psi_walls(const Real *__restrict__ pop, Real *__restrict__ dn,
+                                                          Real *__restrict__ psi,
+                                                          const unsigned char *__restrict__ walls,
+                                                          const Real *__restrict__ psi_w, Geometry<Real> geo,
+                                                          Real rho0, int psi_kind) {
+    const int64_t V = geo.V;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < V; g += (int64_t)gridDim.x * blockDim.x) {
+        if (walls[g] != 1) {
+            psi[g] = psi_w[g];  // walls keep the psi they were given
+            continue;
+        }
+        Real s = pop[(int64_t)lex_q<L::Q>(0) * V + g];
+#pragma unroll
+        for (int i = 1; i < L::Q; i++) s += pop[(int64_t)lex_q<L::Q>(i) * V + g];
+        dn[g] = s;
+        psi[g] = psi_of<Real>(psi_kind, rho0 + s);
+    }
+}
+
+template <class L, class S, bool MRT, class Real, bool STRICT>
+__global__ void __launch_bounds__(128) k_fcs_walls(const Real *__restrict__ pop, Real *__restrict__ pop_out,
+                                                  const Real *__restrict__ dn, const Real *__restrict__ psi,
+                                                  const unsigned char *__restrict__ walls,
+                                                  const __grid_constant__ StepParams<L, S, Real> p) {
+    constexpr int D = L::D, Q = L::Q;
+    const int64_t V = p.geo.V;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < V; g += (int64_t)gridDim.x * blockDim.x) {
+        Real f[Q];
+#pragma unroll
+        for (int q = 0; q < Q; q++) f[q] = __ldg(pop + (int64_t)q * V + g);
+        if (walls[g] != 1) {
+#pragma unroll
+            for (int q = 0; q < Q; q++) pop_out[(int64_t)q * V + g] = f[q];
+            continue;
+        }
+        Cell<D> c;
+        cell_of<D>(g, p.geo.L, c);
+        const Real d = __ldg(dn + g);
+        const Real n = p.rho0 + d;
+        Real F[D], u[D];
+        force_velocity<L, S, Real, STRICT>(psi, c, g, p, f, n, F, u);
+        Real out[Q];
+#pragma unroll
+        for (int q = 0; q < Q; q++) collide_cell<L, S, MRT, Real, STRICT>(f, d, n, u, F, q, p, out[q]);
+        if constexpr (std::is_same<Real, float>::value) {
+            Real rest = d;
+#pragma unroll
+            for (int q = 1; q < Q; q++) rest = __fsub_rn(rest, out[q]);
+            out[0] = rest;
+        }
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            int64_t dst = index_at<D>(c, L::xi(q, 0), L::xi(q, 1), D == 3 ? L::xi(q, 2) : 0, p.geo.L);
+            int qd = q;
+            if (q != 0 && walls[dst] == 0) {
+                dst = g;
+                qd = opposite_q<L>(q);
+            }
+            pop_out[(int64_t)qd * V + dst] = out[q];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // moments read-back: Guo-shifted velocity (and n) after the force
 // ---------------------------------------------------------------------------
 template <class L, class S, class Real, bool STRICT>

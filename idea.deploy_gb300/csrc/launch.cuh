@@ -42,6 +42,11 @@ struct KernelOps {
                        const void *step_params, int grid, cudaStream_t st);
     cudaError_t (*velocity)(const void *pop, const void *dn, const void *psi, void *u,
                             const void *step_params, int grid, cudaStream_t st);
+    // walls (flags 1 fluid / 0 wall, the walls' psi): density pass and fused step
+    cudaError_t (*density_walls)(const void *pop, void *dn, void *psi, const unsigned char *walls, const void *psi_w,
+                                 const void *step_params, int grid, cudaStream_t st);
+    cudaError_t (*fcs_walls)(const void *pop, void *pop_out, const void *dn, const void *psi,
+                             const unsigned char *walls, const void *step_params, int grid, cudaStream_t st);
     cudaError_t (*init_pop)(void *pop, const void *dn, const void *u, const void *eq_params, int grid,
                             cudaStream_t st);
     // occupancy-derived grid sizes (blocks) for a device with `sms` SMs
@@ -125,6 +130,20 @@ struct Ops {
                                 cudaStream_t st) {
         k_velocity<L, S, Real, STRICT><<<grid, 128, 0, st>>>((const Real *)pop, (const Real *)dn, (const Real *)psi,
                                                           (Real *)u, *static_cast<const SP *>(sp));
+        return cudaGetLastError();
+    }
+    static cudaError_t density_walls(const void *pop, void *dn, void *psi, const unsigned char *walls,
+                                     const void *psi_w, const void *sp, int grid, cudaStream_t st) {
+        const SP *p = static_cast<const SP *>(sp);
+        k_density_psi_walls<L, Real><<<grid, 256, 0, st>>>((const Real *)pop, (Real *)dn, (Real *)psi, walls,
+                                                           (const Real *)psi_w, p->geo, p->rho0, p->psi_kind);
+        return cudaGetLastError();
+    }
+    static cudaError_t fcs_walls(const void *pop, void *pop_out, const void *dn, const void *psi,
+                                 const unsigned char *walls, const void *sp, int grid, cudaStream_t st) {
+        k_fcs_walls<L, S, MRT, Real, STRICT><<<grid, 128, 0, st>>>((const Real *)pop, (Real *)pop_out,
+                                                                   (const Real *)dn, (const Real *)psi, walls,
+                                                                   *static_cast<const SP *>(sp));
         return cudaGetLastError();
     }
     static cudaError_t init_pop(void *pop, const void *dn, const void *u, const void *ep, int grid, cudaStream_t st) {
@@ -241,7 +260,7 @@ struct Ops {
         constexpr bool f32 = std::is_same<Real, float>::value;
         using SH = FusedShape<L, S>;
         static const KernelOps o = {sizeof(SP), sizeof(EP), f32 ? 1 : 2, &fill_step, &fill_eq, &density,
-                                    &fcs, &velocity, &init_pop, &grids,
+                                    &fcs, &velocity, &density_walls, &fcs_walls, &init_pop, &grids,
                                     f32 ? &fused : nullptr, SH::TX, SH::TY, SH::R,
                                     f32 ? &fused_occupancy : nullptr,
                                     f32 ? &batch_step : nullptr, f32 ? &batch_density : nullptr,

@@ -231,6 +231,8 @@ struct sclbm_sim {
     void *pop[2] = {nullptr, nullptr};
     int cur = 0;
     void *dn = nullptr, *psi = nullptr, *u = nullptr, *u_old = nullptr;
+    unsigned char *walls = nullptr;  // GetWalls: 1 fluid, 0 wall (null: no walls)
+    void *psi_w = nullptr;           // the psi the walls keep
     double *red = nullptr;
     int red_blocks = 0;
     int dgrid = 0, fgrid = 0, ugrid = 0;
@@ -271,7 +273,7 @@ int alloc(sclbm_sim *s, void **p, size_t bytes) {
 void release(sclbm_sim *s) {
     for (auto &g : s->graph)
         if (g) cudaGraphExecDestroy(g), g = nullptr;
-    for (void *p : {s->pop[0], s->pop[1], s->dn, s->psi, s->u, s->u_old, (void *)s->red})
+    for (void *p : {s->pop[0], s->pop[1], s->dn, s->psi, s->u, s->u_old, (void *)s->red, (void *)s->walls, s->psi_w})
         if (p) cudaFree(p);
     for (auto &ev : s->stage_ev)
         if (ev) cudaEventDestroy(ev), ev = nullptr;
@@ -320,7 +322,14 @@ int stencil_order(int D, const int *e, int qe) {
 bool fused_fits(const sclbm_sim *s) { return (int64_t)s->Q * s->V < ((int64_t)1 << 31); }
 
 bool fused_path(const sclbm_sim *s) {
-    return s->ops->fused != nullptr && s->path != SCLBM_PATH_TWO_PASS && fused_fits(s);
+    return s->ops->fused != nullptr && s->path != SCLBM_PATH_TWO_PASS && fused_fits(s) && !s->walls;
+}
+
+// density + psi of the current populations (fluid cells only with walls)
+cudaError_t density_pass(sclbm_sim *s) {
+    if (s->walls)
+        return s->ops->density_walls(s->pop[s->cur], s->dn, s->psi, s->walls, s->psi_w, s->sp.data(), s->dgrid, s->st);
+    return s->ops->density(s->pop[s->cur], s->dn, s->psi, s->sp.data(), s->dgrid, s->st);
 }
 
 // enqueue the kernels of one step; ev (optional) gets an event after each kernel
@@ -331,9 +340,12 @@ int launch_step(sclbm_sim *s, cudaEvent_t *ev = nullptr) {
         e = o->fused(s->pop[s->cur], s->pop[s->cur ^ 1], s->sp.data(), s->fg, s->fused_grid, s->st);
         if (ev && e == cudaSuccess) e = cudaEventRecord(ev[0], s->st);
     } else {
-        e = o->density(s->pop[s->cur], s->dn, s->psi, s->sp.data(), s->dgrid, s->st);
+        e = density_pass(s);
         if (ev && e == cudaSuccess) e = cudaEventRecord(ev[0], s->st);
-        if (e == cudaSuccess)
+        if (e == cudaSuccess && s->walls)
+            e = o->fcs_walls(s->pop[s->cur], s->pop[s->cur ^ 1], s->dn, s->psi, s->walls, s->sp.data(), s->fgrid,
+                             s->st);
+        else if (e == cudaSuccess)
             e = o->fcs(s->pop[s->cur], s->pop[s->cur ^ 1], s->dn, s->psi, s->sp.data(), s->fgrid, s->st);
         if (ev && e == cudaSuccess) e = cudaEventRecord(ev[1], s->st);
     }
@@ -609,7 +621,7 @@ int configure(sclbm_sim *s, int collision, double tau, const double *mrt_s, cons
 // density at the start of the last step; here it is always the current one).
 int ensure_density(sclbm_sim *s) {
     if (s->dn_fresh || !s->pop_set) return SCLBM_OK;
-    cudaError_t e = s->ops->density(s->pop[s->cur], s->dn, s->psi, s->sp.data(), s->dgrid, s->st);
+    cudaError_t e = density_pass(s);
     if (e != cudaSuccess) return fail(SCLBM_ERR_CUDA, "density: %s", cudaGetErrorString(e));
     s->dn_fresh = true;
     return SCLBM_OK;
@@ -945,7 +957,7 @@ int sclbm_compute_moments(sclbm_sim *s) {
     if (!s) return fail(SCLBM_ERR_ARG, "null handle");
     if (!s->pop_set) return fail(SCLBM_ERR_STATE, "populations are not initialized");
     DevGuard dg(s->device);
-    cudaError_t e = s->ops->density(s->pop[s->cur], s->dn, s->psi, s->sp.data(), s->dgrid, s->st);
+    cudaError_t e = density_pass(s);
     if (e == cudaSuccess) e = s->ops->velocity(s->pop[s->cur], s->dn, s->psi, s->u, s->sp.data(), s->fgrid, s->st);
     if (e != cudaSuccess) return fail(SCLBM_ERR_CUDA, "moments: %s", cudaGetErrorString(e));
     CUDA_TRY(cudaStreamSynchronize(s->st));
@@ -1037,6 +1049,30 @@ int sclbm_density_at(sclbm_sim *s, const int64_t *idx, int count, double *out) {
             CUDA_TRY(cudaStreamSynchronize(s->st));
         }
     }
+    return SCLBM_OK;
+}
+
+int sclbm_set_walls(sclbm_sim *s, const int *walls, const double *psi) {
+    if (!s || !walls || !psi) return fail(SCLBM_ERR_ARG, "null argument");
+    for (int64_t g = 0; g < s->V; g++)
+        if (walls[g] != 0 && walls[g] != 1) return fail(SCLBM_ERR_ARG, "walls[%lld] = %d (1 fluid, 0 wall)",
+                                                        (long long)g, walls[g]);
+    DevGuard dg(s->device);
+    int rc = SCLBM_OK;
+    if (!s->walls) rc = alloc(s, (void **)&s->walls, (size_t)s->V);
+    if (!rc && !s->psi_w) rc = alloc(s, &s->psi_w, (size_t)s->V * s->rs);
+    if (rc) return rc;
+    std::vector<unsigned char> w(s->V);
+    for (int64_t g = 0; g < s->V; g++) w[g] = (unsigned char)walls[g];
+    CUDA_TRY(cudaMemcpyAsync(s->walls, w.data(), s->V, cudaMemcpyHostToDevice, s->st));
+    CUDA_TRY(cudaStreamSynchronize(s->st));
+    // the walls' psi, and the psi array as the reference's GetWalls leaves it
+    rc = h2d_real(s, s->psi_w, psi, s->V, nullptr, 0);
+    if (!rc) rc = h2d_real(s, s->psi, psi, s->V, nullptr, 0);
+    if (rc) return rc;
+    for (auto &g : s->graph)
+        if (g) cudaGraphExecDestroy(g), g = nullptr;  // the step's kernels change
+    s->moments_fresh = s->dn_fresh = false;
     return SCLBM_OK;
 }
 

@@ -270,6 +270,23 @@ class ShanChenMultiPhase:
             self._collision = key
         return self._loop(time_steps, convergence_functions, profiling)
 
+    def GetWalls(self, walls, psi_w):
+        """Wall flags (1 fluid, 0 wall; shape flip(dim_sizes)) and the psi
+        field the walls keep (idpy/LBM/MultiPhase.py:157-162,
+        idpy/LBM/LBM.py:609-631)."""
+        walls = np.asarray(walls)
+        if list(walls.shape) != list(self._flip()):
+            raise Exception("walls must have shape %s" % (self._flip(),))
+        self._sim.set_walls(walls, np.asarray(psi_w, np.float64))
+        self._walls = True
+
+    def MainLoopWalls(self, time_steps, convergence_functions=[], profiling=False):
+        """MainLoop with the walls of GetWalls (idpy/LBM/MultiPhase.py:1226-1309):
+        density and psi on fluid cells, halfway bounce-back at the walls."""
+        if not getattr(self, '_walls', False):
+            raise Exception("Walls not set (GetWalls)")
+        return self.MainLoop(time_steps, convergence_functions, profiling)
+
     # ---- read-back / observables --------------------------------------------
     def ComputeMomentsMeta(self):
         if not self.init_status['pop']:

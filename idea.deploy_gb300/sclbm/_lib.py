@@ -96,6 +96,7 @@ SIGNATURES = {
     'sclbm_batch_init_lattice': [_P, ctypes.c_int],
     'sclbm_batch_probe': [_P, _P, _P],
     'sclbm_restore_mass': [_P, _D, _DP],
+    'sclbm_set_walls': [_P, _P, _P],
     'sclbm_mlp_param_count': [_IP],
     'sclbm_mlp_create': [ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(_P)],
     'sclbm_mlp_destroy': [_P],
@@ -315,6 +316,13 @@ class Sim:
         out = np.empty(idx.size)
         call('sclbm_density_at', self.h, idx.ctypes.data_as(_I64P), int(idx.size), dptr(out))
         return out
+
+    def set_walls(self, walls, psi):
+        """Wall flags (1 fluid, 0 wall) and the psi field the walls keep."""
+        w = np.ascontiguousarray(np.asarray(walls, np.int32).ravel())
+        p = np.ascontiguousarray(np.asarray(psi, np.float64).ravel())
+        assert w.size == self.V and p.size == self.V
+        call('sclbm_set_walls', self.h, ptr(w), ptr(p))
 
     def restore_mass(self, target=float('nan')):
         """FP64 mass before; if target is finite, restore it (rest populations)."""

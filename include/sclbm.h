@@ -149,6 +149,14 @@ SCLBM_API int sclbm_init_single_flat(sclbm_sim *s, double n_g, double n_l, int d
 SCLBM_API int sclbm_init_cylinder(sclbm_sim *s, double n_g, double n_l, double R, int direction,
                         int full_flag);
 
+/* walls (GetWalls, idpy/LBM/MultiPhase.py:157-162, and then every step as
+ * MainLoopWalls, :1226-1309): walls[V] = 1 fluid, 0 wall; psi[V] the psi
+ * field, which wall cells keep (their wetting).  From then on density and psi
+ * are computed on fluid cells only, the step runs on fluid cells only and a
+ * population pushed into a wall returns to the opposite population of its own
+ * cell (halfway bounce-back); the two-pass kernels run (no single pass). */
+SCLBM_API int sclbm_set_walls(sclbm_sim *s, const int *walls, const double *psi);
+
 /* time stepping: enqueue nsteps steps on the handle's stream (returns without
  * waiting); sclbm_sync waits for everything enqueued on the handle */
 SCLBM_API int sclbm_step(sclbm_sim *s, int64_t nsteps);

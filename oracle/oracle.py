@@ -429,10 +429,24 @@ class OracleSim:
         lib().orc_init_populations(ctypes.byref(self.cfg_eq), _ptr(self.n), _ptr(self.u),
                                    _ptr(self.pop))
 
+    def set_walls(self, walls, psi_w):
+        """GetWalls (idpy/LBM/MultiPhase.py:157-162): flags (1 fluid, 0 wall,
+        shape flip(dims)) and the psi field the walls keep."""
+        self.walls = np.ascontiguousarray(np.asarray(walls, np.int32).ravel())
+        self.psi_arr[:] = np.asarray(psi_w, np.float64).ravel()
+        opp = [self.xi.index(tuple(-v for v in x)) for x in self.xi]
+        self.opposite = np.array(opp, np.int32)
+
     def run(self, nsteps):
         sw = ctypes.c_int(0)
-        lib().orc_run(ctypes.byref(self.cfg), _ptr(self.pop), _ptr(self.pop_swap),
-                      _ptr(self.n), _ptr(self.psi_arr), int(nsteps), ctypes.byref(sw))
+        if getattr(self, 'walls', None) is not None:
+            # MainLoopWalls (idpy/LBM/MultiPhase.py:1226-1309)
+            lib().orc_run_walls(ctypes.byref(self.cfg), _ptr(self.pop), _ptr(self.pop_swap), _ptr(self.n),
+                                _ptr(self.psi_arr), _ptr(self.walls), _ptr(self.opposite), int(nsteps),
+                                ctypes.byref(sw))
+        else:
+            lib().orc_run(ctypes.byref(self.cfg), _ptr(self.pop), _ptr(self.pop_swap),
+                          _ptr(self.n), _ptr(self.psi_arr), int(nsteps), ctypes.byref(sw))
         if sw.value:
             self.pop, self.pop_swap = self.pop_swap, self.pop
 

@@ -249,3 +249,65 @@ int orc_run(const orc_cfg *c, double *pop_a, double *pop_b, double *n, double *p
     *swapped = (cur != pop_a);
     return 0;
 }
+
+/* ---- walls (GetWalls / MainLoopWalls, idpy/LBM/MultiPhase.py:157-162,1226-1309) ----
+ * walls[g] = 1 fluid, 0 wall.  Density and psi are computed on fluid cells only
+ * (K_ComputeDensityPsiWallsMeta, MultiPhaseKernelsMeta.py:42-105); wall cells keep
+ * the psi they were given.  The fused step runs on fluid cells only and, for
+ * q != 0, pushes into the opposite population of the same cell when the target
+ * is a wall (SRTCollisionPlusGuoPushStreamWallsCode, Collisions.py:705-860). */
+int orc_density_psi_walls(const orc_cfg *c, const double *pop, const int *walls, double *n, double *psi) {
+    const long V = volume(c);
+    const int Q = c->Q;
+    for (long g = 0; g < V; g++) {
+        if (walls[g] != 1) continue;
+        const double *f = pop + g * Q;
+        double s = f[c->n_order[0]];
+        for (int i = 1; i < Q; i++) s = s + f[c->n_order[i]];
+        psi[g] = psi_of(c->psi_kind, s);
+        n[g] = s;
+    }
+    return 0;
+}
+
+int orc_force_collide_stream_walls(const orc_cfg *c, const double *pop, const double *n, const double *psi,
+                                   const int *walls, const int *opposite, double *pop_swap) {
+    const long V = volume(c);
+    const int Q = c->Q, D = c->dim;
+    double v[1 + 6 + ORC_MAXQ];
+    for (long g = 0; g < V; g++) {
+        if (walls[g] != 1) continue;
+        int x[3];
+        coords(c, g, x);
+        double F[3];
+        sc_force(c, psi, g, x, F);
+        const double *f = pop + g * Q;
+        double u[3];
+        velocity(c, f, n[g], F, u);
+        v[0] = n[g];
+        for (int d = 0; d < D; d++) { v[1 + d] = u[d]; v[1 + D + d] = F[d]; }
+        for (int q = 0; q < Q; q++) v[1 + 2 * D + q] = f[q];
+        for (int q = 0; q < Q; q++) {
+            long dst = neighbour(c, x, c->xi + q * D);
+            int qd = q;
+            if (q != 0 && walls[dst] == 0) {
+                dst = g;
+                qd = opposite[q];
+            }
+            pop_swap[qd + dst * Q] = eval_terms(c, q, v);
+        }
+    }
+    return 0;
+}
+
+int orc_run_walls(const orc_cfg *c, double *pop_a, double *pop_b, double *n, double *psi, const int *walls,
+                  const int *opposite, int nsteps, int *swapped) {
+    double *cur = pop_a, *nxt = pop_b;
+    for (int s = 0; s < nsteps; s++) {
+        orc_density_psi_walls(c, cur, walls, n, psi);
+        orc_force_collide_stream_walls(c, cur, n, psi, walls, opposite, nxt);
+        double *t = cur; cur = nxt; nxt = t;
+    }
+    *swapped = (cur != pop_a);
+    return 0;
+}
