@@ -414,4 +414,54 @@ int build_collision(const CollisionSpec &s, CollisionTables &t, std::string &err
     }
 }
 
+// Noise operator of the fluctuating step (Gross et al. 2011; GrossShanChenMultiPhase,
+// idpy/LBM/Fluctuations.py:40-165): the random moments are the W-orthogonal Hermite
+// moments k = D+1 .. Q-1, so the noise populations are
+//     rpop_q = sum_k Mw^-1[q][k] Rm_{k-D-1}                       (Fluctuations.py:158-163)
+// and moment k has the variance (GetVariances, Fluctuations.py:72-97)
+//     var_k = norm_k kBT (2 - 1/tau) / tau / c_s^2 n0,  norm_k = sum_q w_q Mw[k][q]^2.
+// var_k is evaluated as the reference does: each product and quotient rounded to
+// double (sympy Floats of 53 bits), tau = 1/(1/tau) (the kernel gets tau as
+// 1/OMEGA).  SCLBM_LIT_ROUND15 then prints var_k and each coefficient with 15
+// significant digits; SCLBM_LIT_EXACT keeps var_k and rounds the exact
+// coefficients once to double.
+int build_noise(const CollisionSpec &s, double kBT, double n0, std::vector<double> &m2var,
+                std::vector<double> &coef, std::string &err) {
+    try {
+        const int D = s.dim, Q = s.q, NR = Q - D - 1;
+        if (NR <= 0) throw std::domain_error("no random moments");
+        std::vector<Rat> W(Q);
+        for (int i = 0; i < Q; i++) W[i] = recognize(s.w[i]);
+        const Rat c2 = recognize(s.c2);
+        Mat Mn, Mw;
+        hermite_bases(D, Q, s.xi, W, c2, Mn, Mw);
+        const Mat Mwi = inverse(Mw);
+        m2var.assign(NR, 0.0);
+        coef.assign((size_t)Q * NR, 0.0);
+        const double tau = 1.0 / (1.0 / s.tau);
+        for (int j = 0; j < NR; j++) {
+            const int k = D + 1 + j;
+            Rat norm(0);
+            for (int q = 0; q < Q; q++) norm = norm + W[q] * Mw[k][q] * Mw[k][q];
+            double var = to_double(norm) * kBT;
+            var = var * (2.0 - 1.0 / tau);
+            var = var / tau;
+            var = var / s.c2;
+            var = var * n0;
+            if (s.literals == 0 && var != 0.0) {
+                char buf[40];
+                std::snprintf(buf, sizeof buf, "%.14e", var);
+                var = std::strtod(buf, nullptr);
+            }
+            m2var[j] = -2.0 * var;
+            for (int q = 0; q < Q; q++)
+                coef[(size_t)q * NR + j] = s.literals == 0 ? round_sig(Mwi[q][k], 15) : to_double(Mwi[q][k]);
+        }
+        return 0;
+    } catch (const std::exception &e) {
+        err = e.what();
+        return 1;
+    }
+}
+
 }  // namespace sclbm

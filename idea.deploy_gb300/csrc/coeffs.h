@@ -28,4 +28,9 @@ struct CollisionTables {
 
 int build_collision(const CollisionSpec &s, CollisionTables &t, std::string &err);
 
+// noise operator of the fluctuating (Gross 2011) step: m2var[j] = -2 var_j and
+// coef[q*NR + j], the weight of random moment j in noise population q (NR = q-dim-1)
+int build_noise(const CollisionSpec &s, double kBT, double n0, std::vector<double> &m2var,
+                std::vector<double> &coef, std::string &err);
+
 }  // namespace sclbm

@@ -12,6 +12,7 @@
 #include "batch.cuh"
 #include "fused.cuh"
 #include "kernels.cuh"
+#include "noise.cuh"
 
 namespace sclbm {
 
@@ -70,6 +71,12 @@ struct KernelOps {
                                   cudaStream_t st);
     cudaError_t (*batch_probe)(const void *pop, const BatchInst *inst, int n_inst, int Vtot, double *out,
                                cudaStream_t st);
+    // fluctuating step (BGK only, else null): parameter block, its filler from the
+    // noise operator (m2var[nr], coef[q*nr]) and the launcher; grid from occupancy
+    size_t noise_size;
+    void (*fill_noise)(void *params, int kind, int indep, const double *m2var, const double *coef);
+    cudaError_t (*fcs_noise)(const void *pop, void *pop_out, const void *dn, const void *psi, void *seeds,
+                             const void *step_params, const void *noise_params, int sms, cudaStream_t st);
 };
 
 template <class L, class S, bool MRT, class Real, bool STRICT>
@@ -256,6 +263,32 @@ struct Ops {
         }
         return cudaErrorNotSupported;
     }
+    using NP = NoiseParams<L, Real>;
+    static void fill_noise(void *params, int kind, int indep, const double *m2var, const double *coef) {
+        NP *z = static_cast<NP *>(params);
+        std::memset(z, 0, sizeof(NP));
+        z->kind = kind;
+        z->indep = indep;
+        for (int k = 0; k < NP::NR; k++) z->m2var[k] = (Real)m2var[k];
+        for (int q = 0; q < Q; q++)
+            for (int k = 0; k < NP::NR; k++) z->coef[q][k] = (Real)coef[q * NP::NR + k];
+    }
+    static cudaError_t fcs_noise(const void *pop, void *pop_out, const void *dn, const void *psi, void *seeds,
+                                 const void *sp, const void *np, int sms, cudaStream_t st) {
+        if constexpr (!MRT) {
+            static int per_sm = 0;
+            if (!per_sm) {
+                int b = 0;
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fcs_noise<L, S, Real, STRICT>, 128, 0);
+                per_sm = b > 0 ? b : 1;
+            }
+            k_fcs_noise<L, S, Real, STRICT><<<sms * per_sm, 128, 0, st>>>(
+                (const Real *)pop, (Real *)pop_out, (const Real *)dn, (const Real *)psi, seeds,
+                *static_cast<const SP *>(sp), *static_cast<const NP *>(np));
+            return cudaGetLastError();
+        }
+        return cudaErrorNotSupported;
+    }
     static const KernelOps *ops() {
         constexpr bool f32 = std::is_same<Real, float>::value;
         using SH = FusedShape<L, S>;
@@ -265,7 +298,8 @@ struct Ops {
                                     f32 ? &fused_occupancy : nullptr,
                                     f32 ? &batch_step : nullptr, f32 ? &batch_density : nullptr,
                                     f32 ? &batch_moments : nullptr, f32 ? &batch_mass : nullptr,
-                                    f32 ? &batch_add_rest : nullptr, f32 ? &batch_probe : nullptr};
+                                    f32 ? &batch_add_rest : nullptr, f32 ? &batch_probe : nullptr,
+                                    sizeof(NP), MRT ? nullptr : &fill_noise, MRT ? nullptr : &fcs_noise};
         return &o;
     }
 };

@@ -233,6 +233,13 @@ struct sclbm_sim {
     void *dn = nullptr, *psi = nullptr, *u = nullptr, *u_old = nullptr;
     unsigned char *walls = nullptr;  // GetWalls: 1 fluid, 0 wall (null: no walls)
     void *psi_w = nullptr;           // the psi the walls keep
+    // fluctuations (sclbm_set_fluctuations): generator kind (0: off), one or two
+    // generators per random moment, their states on the device, the noise operator
+    int noise_kind = 0, noise_indep = 0, noise_streams = 0;
+    void *seeds = nullptr;
+    std::vector<double> noise_m2var, noise_coef;
+    std::vector<unsigned char> np;  // noise launch parameter block
+    double tau_bgk = 1.0;           // BGK relaxation time of the current operator
     double *red = nullptr;
     int red_blocks = 0;
     int dgrid = 0, fgrid = 0, ugrid = 0;
@@ -273,7 +280,8 @@ int alloc(sclbm_sim *s, void **p, size_t bytes) {
 void release(sclbm_sim *s) {
     for (auto &g : s->graph)
         if (g) cudaGraphExecDestroy(g), g = nullptr;
-    for (void *p : {s->pop[0], s->pop[1], s->dn, s->psi, s->u, s->u_old, (void *)s->red, (void *)s->walls, s->psi_w})
+    for (void *p : {s->pop[0], s->pop[1], s->dn, s->psi, s->u, s->u_old, (void *)s->red, (void *)s->walls, s->psi_w,
+                    s->seeds})
         if (p) cudaFree(p);
     for (auto &ev : s->stage_ev)
         if (ev) cudaEventDestroy(ev), ev = nullptr;
@@ -322,7 +330,8 @@ int stencil_order(int D, const int *e, int qe) {
 bool fused_fits(const sclbm_sim *s) { return (int64_t)s->Q * s->V < ((int64_t)1 << 31); }
 
 bool fused_path(const sclbm_sim *s) {
-    return s->ops->fused != nullptr && s->path != SCLBM_PATH_TWO_PASS && fused_fits(s) && !s->walls;
+    return s->ops->fused != nullptr && s->path != SCLBM_PATH_TWO_PASS && fused_fits(s) && !s->walls &&
+           !s->noise_kind;
 }
 
 // density + psi of the current populations (fluid cells only with walls)
@@ -342,7 +351,10 @@ int launch_step(sclbm_sim *s, cudaEvent_t *ev = nullptr) {
     } else {
         e = density_pass(s);
         if (ev && e == cudaSuccess) e = cudaEventRecord(ev[0], s->st);
-        if (e == cudaSuccess && s->walls)
+        if (e == cudaSuccess && s->noise_kind)
+            e = o->fcs_noise(s->pop[s->cur], s->pop[s->cur ^ 1], s->dn, s->psi, s->seeds, s->sp.data(), s->np.data(),
+                             s->sms, s->st);
+        else if (e == cudaSuccess && s->walls)
             e = o->fcs_walls(s->pop[s->cur], s->pop[s->cur ^ 1], s->dn, s->psi, s->walls, s->sp.data(), s->fgrid,
                              s->st);
         else if (e == cudaSuccess)
@@ -584,6 +596,8 @@ int configure(sclbm_sim *s, int collision, double tau, const double *mrt_s, cons
     const bool strict = !s->fp32 && s->literals == SCLBM_LIT_ROUND15;
     const KernelOps *ops = select_ops(s->D, s->order, mrt, s->fp32, strict);
     if (!ops) return fail(SCLBM_ERR_UNSUPPORTED, "no kernels for this configuration");
+    if (s->noise_kind && !ops->fcs_noise)
+        return fail(SCLBM_ERR_UNSUPPORTED, "the fluctuating step is BGK only (switch the fluctuations off first)");
     bool a_nonzero = false;
     for (int q = 0; q < s->Q; q++) a_nonzero = a_nonzero || t.A[(size_t)q * s->Q + q] != 0.0;
     HostSetup h;
@@ -608,6 +622,12 @@ int configure(sclbm_sim *s, int collision, double tau, const double *mrt_s, cons
     s->ep.assign(ops->eq_size, 0);
     ops->fill_step(s->sp.data(), h);
     ops->fill_eq(s->ep.data(), h);
+    s->tau_bgk = h.omega > 0 ? 1.0 / h.omega : 1.0;
+    if (collision == SCLBM_COLL_BGK && !coll_a && !(uniform_rate > 0)) s->tau_bgk = tau;
+    if (s->noise_kind) {
+        s->np.assign(ops->noise_size, 0);
+        ops->fill_noise(s->np.data(), s->noise_kind, s->noise_indep, s->noise_m2var.data(), s->noise_coef.data());
+    }
     ops->grids(s->sms, &s->dgrid, &s->fgrid);
     const int64_t need_d = (s->V + 255) / 256, need_f = (s->V + 127) / 128;
     s->dgrid = (int)std::max<int64_t>(1, std::min<int64_t>(s->dgrid, need_d));
@@ -1054,6 +1074,7 @@ int sclbm_density_at(sclbm_sim *s, const int64_t *idx, int count, double *out) {
 
 int sclbm_set_walls(sclbm_sim *s, const int *walls, const double *psi) {
     if (!s || !walls || !psi) return fail(SCLBM_ERR_ARG, "null argument");
+    if (s->noise_kind) return fail(SCLBM_ERR_UNSUPPORTED, "walls with fluctuations (the reference has no such step)");
     for (int64_t g = 0; g < s->V; g++)
         if (walls[g] != 0 && walls[g] != 1) return fail(SCLBM_ERR_ARG, "walls[%lld] = %d (1 fluid, 0 wall)",
                                                         (long long)g, walls[g]);
@@ -1073,6 +1094,127 @@ int sclbm_set_walls(sclbm_sim *s, const int *walls, const double *psi) {
     for (auto &g : s->graph)
         if (g) cudaGraphExecDestroy(g), g = nullptr;  // the step's kernels change
     s->moments_fresh = s->dn_fresh = false;
+    return SCLBM_OK;
+}
+
+int sclbm_noise_counts(int dim, int q, int indep, int *moments, int *streams) {
+    if (dim < 1 || q <= dim + 1) return fail(SCLBM_ERR_ARG, "dim %d, q %d", dim, q);
+    const int nr = q - dim - 1;
+    if (moments) *moments = nr;
+    if (streams) *streams = indep ? 2 * nr : nr;
+    return SCLBM_OK;
+}
+
+int sclbm_noise_operator(const sclbm_params *p, double kBT, double n0, double *m2var, double *coef) {
+    if (!p || !p->xi || !p->w || !m2var || !coef) return fail(SCLBM_ERR_ARG, "null argument");
+    if ((p->dim != 2 && p->dim != 3) || p->q <= p->dim + 1) return fail(SCLBM_ERR_ARG, "dim %d, q %d", p->dim, p->q);
+    if (!(p->tau > 0) || !(kBT >= 0) || !std::isfinite(kBT) || !std::isfinite(n0))
+        return fail(SCLBM_ERR_ARG, "tau %g, kBT %g, n0 %g", p->tau, kBT, n0);
+    CollisionSpec cs;
+    cs.dim = p->dim;
+    cs.q = p->q;
+    cs.xi = p->xi;
+    cs.w = p->w;
+    cs.c2 = p->c2;
+    cs.tau = p->tau;
+    cs.literals = p->literals;
+    std::vector<double> mv, cf;
+    std::string err;
+    if (build_noise(cs, kBT, n0, mv, cf, err)) return fail(SCLBM_ERR_UNSUPPORTED, "noise operator: %s", err.c_str());
+    std::copy(mv.begin(), mv.end(), m2var);
+    std::copy(cf.begin(), cf.end(), coef);
+    return SCLBM_OK;
+}
+
+int sclbm_set_fluctuations(sclbm_sim *s, int generator, int indep, double kBT, double n0, const void *seeds,
+                           int layout, const double *m2var, const double *coef) {
+    if (!s) return fail(SCLBM_ERR_ARG, "null handle");
+    DevGuard dg(s->device);
+    CUDA_TRY(cudaStreamSynchronize(s->st));
+    for (auto &g : s->graph)
+        if (g) cudaGraphExecDestroy(g), g = nullptr;  // the step's kernels change
+    if (generator == SCLBM_CRNG_NONE) {
+        if (s->seeds) cudaFree(s->seeds), s->device_bytes -= (int64_t)s->noise_streams * s->V *
+                                                             (s->noise_kind == SCLBM_CRNG_MMIX ? 8 : 4);
+        s->seeds = nullptr;
+        s->noise_kind = s->noise_streams = 0;
+        return SCLBM_OK;
+    }
+    if (generator != SCLBM_CRNG_MINSTD && generator != SCLBM_CRNG_NUMREC && generator != SCLBM_CRNG_MMIX)
+        return fail(SCLBM_ERR_ARG, "generator %d", generator);
+    if (!seeds) return fail(SCLBM_ERR_ARG, "null seeds");
+    if (layout != SCLBM_SEEDS_STREAM_MAJOR && layout != SCLBM_SEEDS_CELL_MAJOR)
+        return fail(SCLBM_ERR_ARG, "seeds layout %d", layout);
+    if ((m2var == nullptr) != (coef == nullptr)) return fail(SCLBM_ERR_ARG, "m2var and coef go together");
+    if (s->mrt || !s->ops->fcs_noise) return fail(SCLBM_ERR_UNSUPPORTED, "the fluctuating step is BGK only");
+    if (s->walls) return fail(SCLBM_ERR_UNSUPPORTED, "walls with fluctuations (the reference has no such step)");
+    if (!(kBT >= 0) || !std::isfinite(kBT) || !std::isfinite(n0)) return fail(SCLBM_ERR_ARG, "kBT %g, n0 %g", kBT, n0);
+    const int nr = s->Q - s->D - 1, ns = indep ? 2 * nr : nr;
+    std::vector<double> mv, cf;
+    if (m2var) {
+        mv.assign(m2var, m2var + nr);
+        cf.assign(coef, coef + (size_t)s->Q * nr);
+    } else {
+        CollisionSpec cs;
+        cs.dim = s->D;
+        cs.q = s->Q;
+        cs.xi = s->xi.data();
+        cs.w = s->w.data();
+        cs.c2 = s->c2;
+        cs.tau = s->tau_bgk;
+        cs.literals = s->fp32 ? SCLBM_LIT_EXACT : s->literals;
+        std::string err;
+        if (build_noise(cs, kBT, n0, mv, cf, err)) return fail(SCLBM_ERR_UNSUPPORTED, "noise operator: %s", err.c_str());
+    }
+    for (double v : mv)
+        if (!std::isfinite(v) || v > 0) return fail(SCLBM_ERR_ARG, "m2var must be finite and <= 0");
+    // generator states: uint64 for MMIX, uint32 otherwise; stored stream-major
+    const size_t es = generator == SCLBM_CRNG_MMIX ? 8 : 4;
+    const size_t bytes = (size_t)ns * s->V * es;
+    if (s->seeds && (size_t)s->noise_streams * s->V * (s->noise_kind == SCLBM_CRNG_MMIX ? 8 : 4) != bytes) {
+        cudaFree(s->seeds);
+        s->device_bytes -= (int64_t)s->noise_streams * s->V * (s->noise_kind == SCLBM_CRNG_MMIX ? 8 : 4);
+        s->seeds = nullptr;
+    }
+    if (!s->seeds) {
+        int rc = alloc(s, &s->seeds, bytes);
+        if (rc) return rc;
+    }
+    std::vector<unsigned char> host(bytes);
+    for (int64_t g = 0; g < s->V; g++)
+        for (int k = 0; k < ns; k++) {
+            const size_t src = layout == SCLBM_SEEDS_STREAM_MAJOR ? (size_t)k * s->V + g : (size_t)g * ns + k;
+            const size_t dst = (size_t)k * s->V + g;
+            std::memcpy(host.data() + dst * es, (const unsigned char *)seeds + src * es, es);
+        }
+    CUDA_TRY(cudaMemcpyAsync(s->seeds, host.data(), bytes, cudaMemcpyHostToDevice, s->st));
+    CUDA_TRY(cudaStreamSynchronize(s->st));
+    s->noise_kind = generator;
+    s->noise_indep = indep ? 1 : 0;
+    s->noise_streams = ns;
+    s->noise_m2var = mv;
+    s->noise_coef = cf;
+    s->np.assign(s->ops->noise_size, 0);
+    s->ops->fill_noise(s->np.data(), s->noise_kind, s->noise_indep, mv.data(), cf.data());
+    return SCLBM_OK;
+}
+
+int sclbm_get_seeds(sclbm_sim *s, void *seeds, int layout) {
+    if (!s || !seeds) return fail(SCLBM_ERR_ARG, "null argument");
+    if (!s->noise_kind) return fail(SCLBM_ERR_STATE, "no fluctuations set");
+    if (layout != SCLBM_SEEDS_STREAM_MAJOR && layout != SCLBM_SEEDS_CELL_MAJOR)
+        return fail(SCLBM_ERR_ARG, "seeds layout %d", layout);
+    DevGuard dg(s->device);
+    const size_t es = s->noise_kind == SCLBM_CRNG_MMIX ? 8 : 4, ns = (size_t)s->noise_streams;
+    std::vector<unsigned char> host(ns * s->V * es);
+    CUDA_TRY(cudaMemcpyAsync(host.data(), s->seeds, host.size(), cudaMemcpyDeviceToHost, s->st));
+    CUDA_TRY(cudaStreamSynchronize(s->st));
+    for (int64_t g = 0; g < s->V; g++)
+        for (size_t k = 0; k < ns; k++) {
+            const size_t src = k * s->V + g;
+            const size_t dst = layout == SCLBM_SEEDS_STREAM_MAJOR ? k * s->V + g : g * ns + k;
+            std::memcpy((unsigned char *)seeds + dst * es, host.data() + src * es, es);
+        }
     return SCLBM_OK;
 }
 

@@ -15,8 +15,20 @@ the reference's 'gpu' ordering); ``lang`` is accepted but there is one
 backend, with no CPU fallback.  Extra keywords: ``precision`` ('fp64' or
 'fp32_shifted'; ``fp32_flag=True`` selects the latter), ``rho0`` (shift of
 the FP32 storage), ``literals`` ('round15' as the reference prints them, or
-'exact'), ``collision_tables`` ((A, B) explicit operator, see include/sclbm.h).
+'exact'), ``collision_tables`` ((A, B) explicit operator, see include/sclbm.h),
+``noise_tables`` ((m2var, coef) explicit noise operator of the fluctuating step).
+
+Fluctuations (``fluctuations='Gross2011'`` with ``prng_kind``, ``init_seed``,
+``prng_init_from``, ``prng_distribution``, ``indep_gaussian``, then
+``MainLoopGross2011SRT``, idpy/LBM/MultiPhase.py:1404-1541,2029-2069): the
+generator states are drawn as the reference's CRNGS draws them
+(idpy/PRNGS/CRNGS.py:289-337, numpy's legacy seeding) and mapped to cells by
+the same ordering, so a run started from the same seed follows the reference's
+random stream.  ``crng.sims_idpy_memory['seeds'].D2H()`` reads them back.  The
+``flat`` distribution is refused: the reference's code generator fails on it
+(its variances are strings, CRNGS.py:903 with Fluctuations.py:87-97).
 """
+import os
 import time
 
 import numpy as np
@@ -170,6 +182,97 @@ class ShanChenMultiPhase:
         self.sims_idpy_memory = {k: _Field(self, k) for k in ('n', 'u', 'pop', 'psi')}
         self.init_status = {'n': False, 'u': False, 'pop': False}
         self.aux_vars = []
+        self.crng = None
+        if p.get('fluctuations') is not None:
+            self._init_fluctuations()
+
+    # ---- fluctuations ------------------------------------------------------------
+    def _init_fluctuations(self):
+        """InitMemory's fluctuation branch (idpy/LBM/MultiPhase.py:2029-2069)."""
+        p = self.params_dict
+        if p['fluctuations'] != 'Gross2011':
+            raise Exception("Parameter 'fluctuations' must be 'Gross2011'")
+        for key in ('prng_kind', 'prng_distribution'):
+            if key not in p:
+                raise Exception("Missing parameter '%s'" % key)
+        if p['prng_kind'] not in _lib.CRNG_KINDS:
+            raise Exception("'prng_kind' must be one of %s" % sorted(_lib.CRNG_KINDS))
+        if p['prng_distribution'] not in ('flat', 'gaussian'):
+            raise Exception("Parameter 'distribution' must be in ['flat', 'gaussian']")
+        if p['prng_distribution'] == 'flat':
+            raise Exception("the 'flat' distribution of the fluctuating step is not available: the "
+                            "reference's code generator fails on it (string variances)")
+        init_from = p.get('prng_init_from', 'numpy')
+        if init_from not in ('numpy', 'urandom'):
+            raise Exception("'init_from' must be either 'numpy' or 'urandom'")
+        indep = bool(p.get('indep_gaussian', False))
+        nr, ns = _lib.noise_counts(self.sims_vars['DIM'], self.sims_vars['Q'], indep)
+        V = self.sims_vars['V']
+        self.crng = CRNGS(p['prng_kind'], ns * V, init_from, p.get('init_seed', 1), self)
+        self.sims_vars['N_PRNG_STREAMS'] = ns
+        self._noise = dict(indep=indep, streams=ns, moments=nr, key=None)
+
+    def _seeds_layout(self):
+        return _lib.SEEDS_CELL_MAJOR if self.params_dict['set_ordering'] == 'cpu' else _lib.SEEDS_STREAM_MAJOR
+
+    def _noise_on(self, kBT, n0):
+        nz = self._noise
+        key = (float(kBT), float(n0), self._collision)
+        if nz['key'] == key:
+            return
+        seeds = self.crng._host_seeds()
+        tables = self.params_dict.get('noise_tables')
+        self._sim.set_fluctuations(self.params_dict['prng_kind'], nz['indep'], kBT, n0, seeds, self._seeds_layout(),
+                                   None if tables is None else tables[0], None if tables is None else tables[1])
+        self.crng._on_device = True
+        nz['key'] = key
+
+    def _noise_off(self):
+        if self.crng is None or self._noise['key'] is None:
+            return
+        self.crng._cache = self._sim.get_seeds(self._seeds_layout())
+        self.crng._on_device = False
+        self._sim.set_fluctuations(None, False, 0.0, 0.0, None)
+        self._noise['key'] = None
+
+    def MainLoopGross2011SRT(self, time_steps, convergence_functions=[], convergence_functions_args=[],
+                             profiling=False, kBT=None, n0=None, print_flag=True):
+        """The fluctuating step of Gross et al. (2011) with the BGK collision
+        (idpy/LBM/MultiPhase.py:1404-1541): every step adds the noise
+        populations of the Gaussian random moments drawn from the cells'
+        generators."""
+        if kBT is None:
+            raise Exception("Missing parameter 'kBT'")
+        elif kBT < 0:
+            raise Exception("Paramter 'kBT' must be positive")
+        if n0 is None:
+            raise Exception("Missing parameter 'n0'")
+        if self.crng is None:
+            raise Exception("Fluctuations not set up: construct with fluctuations='Gross2011'")
+        self._check_init()
+        if self._collision != ('bgk', self.params_dict['tau']):
+            self._sim.set_collision(_lib.COLL_BGK, tau=self.params_dict['tau'])
+            self._collision = ('bgk', self.params_dict['tau'])
+        self._noise_on(kBT, n0)
+        old_step, prof = 0, {}
+        self.sims_vars['time_steps'] = []
+        for step in list(time_steps)[1:]:
+            if print_flag and self.verbose:
+                print("Step:", step)
+            t0 = time.perf_counter()
+            self._sim.step(step - old_step, sync=True)
+            prof[step] = time.perf_counter() - t0
+            self.sims_vars['time_steps'].append(step)
+            old_step = step
+            if len(convergence_functions):
+                if len(convergence_functions_args):
+                    checks = [c_f(self, **convergence_functions_args[i]) for i, c_f in enumerate(convergence_functions)]
+                else:
+                    checks = [c_f(self) for c_f in convergence_functions]
+                if any(checks):
+                    break
+        self.sims_vars['time_steps'] = np.array(self.sims_vars['time_steps'])
+        return prof if profiling else None
 
     # ---- layout helpers ------------------------------------------------------
     def _flip(self):
@@ -251,6 +354,7 @@ class ShanChenMultiPhase:
 
     def MainLoop(self, time_steps, convergence_functions=[], profiling=False):
         self._check_init()
+        self._noise_off()
         if self._collision != ('bgk', self.params_dict['tau']) and self._collision != ('tables',):
             self._sim.set_collision(_lib.COLL_BGK, tau=self.params_dict['tau'])
             self._collision = ('bgk', self.params_dict['tau'])
@@ -263,6 +367,7 @@ class ShanChenMultiPhase:
         if omega_syms_vals is None:
             raise Exception("Missing argument 'omega_syms_vals'")
         self._check_init()
+        self._noise_off()
         S = numeric_relaxation_matrix(relaxation_matrix, omega_syms_vals, self.sims_vars['Q'])
         key = ('mrt', S.tobytes())
         if self._collision != key:
@@ -275,6 +380,7 @@ class ShanChenMultiPhase:
         field the walls keep (idpy/LBM/MultiPhase.py:157-162,
         idpy/LBM/LBM.py:609-631)."""
         walls = np.asarray(walls)
+        self._noise_off()
         if list(walls.shape) != list(self._flip()):
             raise Exception("walls must have shape %s" % (self._flip(),))
         self._sim.set_walls(walls, np.asarray(psi_w, np.float64))
@@ -345,6 +451,60 @@ class ShanChenMultiPhase:
 
     def End(self):
         self._sim.close()
+
+
+class CRNGS:
+    """The generator states of the fluctuating step, drawn as the reference's
+    ``CRNGS.InitSeeds`` draws them (idpy/PRNGS/CRNGS.py:289-337): numpy's
+    legacy generator seeded with ``init_seed`` (one stream), integers in
+    [1, RANDMAX) of the generator's state type, or 4 bytes of ``os.urandom``
+    each; MINSTD states masked to 31 bits.  Entry i of the array belongs to
+    (cell, stream) by the simulation's ordering: 'gpu' i = cell + stream * V,
+    'cpu' i = stream + cell * streams (MultiPhase.py:1962-1965)."""
+    RANDMAX = {'MINSTD': 0x7fffffff, 'NUMREC': 0xffffffff, 'MMIX': 0xffffffffffffffff}
+
+    def __init__(self, kind, n_prngs, init_from, init_seed, owner):
+        self.owner = owner
+        dt = np.uint64 if kind == 'MMIX' else np.uint32
+        if init_from == 'numpy':
+            np.random.seed(int(init_seed))
+            seeds = np.random.randint(low=1, high=self.RANDMAX[kind], size=int(n_prngs), dtype=dt)
+        else:
+            seeds = np.array([int.from_bytes(os.urandom(4), byteorder='big', signed=False)
+                              for _ in range(int(n_prngs))], dt)
+        if kind == 'MINSTD':
+            seeds &= dt(self.RANDMAX[kind])
+        self.sims_vars = {'kind': kind, 'n_prngs': int(n_prngs), 'init_from': init_from,
+                          'init_seed': init_seed, 'ID_RANDMAX': self.RANDMAX[kind], 'n_streams': 1}
+        self.constants = {'ID_RANDMAX': self.RANDMAX[kind], 'N_PRNGS': int(n_prngs)}
+        self._cache = seeds
+        self._on_device = False
+        self.sims_idpy_memory = {'seeds': _SeedsField(self)}
+
+    def _host_seeds(self):
+        if self._on_device:
+            return self.owner._sim.get_seeds(self.owner._seeds_layout())
+        return self._cache
+
+
+class _SeedsField:
+    def __init__(self, crng):
+        self.crng = crng
+
+    def D2H(self):
+        return self.crng._host_seeds().copy()
+
+    def H2D(self, array):
+        c = self.crng
+        a = np.asarray(array).astype(c._cache.dtype).ravel()
+        if a.size != c._cache.size:
+            raise Exception('expected %d generator states' % c._cache.size)
+        c._cache = a.copy()
+        if c._on_device:   # fluctuations running: upload the new states now
+            kBT, n0, _ = c.owner._noise['key']
+            c.owner._noise['key'] = None
+            c._on_device = False
+            c.owner._noise_on(kBT, n0)
 
 
 def numeric_relaxation_matrix(relaxation_matrix, omega_syms_vals, Q):

@@ -17,6 +17,9 @@ PATH_AUTO, PATH_TWO_PASS, PATH_FUSED = 0, 1, 2
 COLL_BGK, COLL_MRT = 0, 1
 FP64, FP32_SHIFTED = 0, 1
 LIT_ROUND15, LIT_EXACT = 0, 1
+CRNG_NONE, CRNG_MINSTD, CRNG_NUMREC, CRNG_MMIX = 0, 1, 2, 3
+CRNG_KINDS = {'MINSTD': CRNG_MINSTD, 'NUMREC': CRNG_NUMREC, 'MMIX': CRNG_MMIX}
+SEEDS_STREAM_MAJOR, SEEDS_CELL_MAJOR = 0, 1
 
 
 class SclbmError(RuntimeError):
@@ -97,6 +100,10 @@ SIGNATURES = {
     'sclbm_batch_probe': [_P, _P, _P],
     'sclbm_restore_mass': [_P, _D, _DP],
     'sclbm_set_walls': [_P, _P, _P],
+    'sclbm_noise_counts': [ctypes.c_int, ctypes.c_int, ctypes.c_int, _IP, _IP],
+    'sclbm_noise_operator': [ctypes.POINTER(Params), _D, _D, _P, _P],
+    'sclbm_set_fluctuations': [_P, ctypes.c_int, ctypes.c_int, _D, _D, _P, ctypes.c_int, _P, _P],
+    'sclbm_get_seeds': [_P, _P, ctypes.c_int],
     'sclbm_mlp_param_count': [_IP],
     'sclbm_mlp_create': [ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(_P)],
     'sclbm_mlp_destroy': [_P],
@@ -324,6 +331,33 @@ class Sim:
         assert w.size == self.V and p.size == self.V
         call('sclbm_set_walls', self.h, ptr(w), ptr(p))
 
+    def set_fluctuations(self, kind, indep, kBT, n0, seeds, layout=SEEDS_STREAM_MAJOR, m2var=None, coef=None):
+        """Gross (2011) fluctuations: generator kind ('MINSTD', 'NUMREC', 'MMIX'
+        or None to switch them off), seeds (uint32 / uint64 for MMIX, V x streams
+        in the given layout), optional explicit operator (m2var[nr], coef[q, nr])."""
+        if kind is None:
+            call('sclbm_set_fluctuations', self.h, CRNG_NONE, 0, 0.0, 0.0, None, 0, None, None)
+            self.noise = None
+            return
+        k = CRNG_KINDS[kind] if isinstance(kind, str) else int(kind)
+        nr, ns = noise_counts(self.dim, self.q, indep)
+        dt = np.uint64 if k == CRNG_MMIX else np.uint32
+        seeds = np.ascontiguousarray(np.asarray(seeds).astype(dt).ravel())
+        assert seeds.size == ns * self.V, (seeds.size, ns * self.V)
+        mv = None if m2var is None else np.ascontiguousarray(np.asarray(m2var, np.float64).ravel())
+        cf = None if coef is None else np.ascontiguousarray(np.asarray(coef, np.float64).ravel())
+        if mv is not None:
+            assert mv.size == nr and cf.size == self.q * nr
+        call('sclbm_set_fluctuations', self.h, k, int(bool(indep)), float(kBT), float(n0), ptr(seeds), int(layout),
+             None if mv is None else ptr(mv), None if cf is None else ptr(cf))
+        self.noise = (k, ns, dt)
+
+    def get_seeds(self, layout=SEEDS_STREAM_MAJOR):
+        k, ns, dt = self.noise
+        out = np.empty(ns * self.V, dt)
+        call('sclbm_get_seeds', self.h, ptr(out), int(layout))
+        return out
+
     def restore_mass(self, target=float('nan')):
         """FP64 mass before; if target is finite, restore it (rest populations)."""
         m = ctypes.c_double()
@@ -338,3 +372,24 @@ class Sim:
 
 def monomial_count(dim):
     return load().sclbm_monomial_count(int(dim))
+
+
+def noise_counts(dim, q, indep):
+    """(random moments, generator states per cell)."""
+    m, n = ctypes.c_int(), ctypes.c_int()
+    call('sclbm_noise_counts', int(dim), int(q), int(bool(indep)), ctypes.byref(m), ctypes.byref(n))
+    return m.value, n.value
+
+
+def noise_operator(dim, xi, w, c2, tau, kBT, n0, literals=LIT_ROUND15):
+    """Host-side noise operator (m2var[nr], coef[q, nr]) for a BGK lattice."""
+    xi_a = np.ascontiguousarray(np.array(xi, np.int32).ravel())
+    w_a = np.ascontiguousarray(np.array(w, np.float64))
+    q = len(w_a)
+    p = Params()
+    p.dim, p.q, p.xi, p.w, p.c2 = int(dim), q, ptr(xi_a), ptr(w_a), float(c2)
+    p.tau, p.literals = float(tau), int(literals)
+    nr = q - int(dim) - 1
+    mv, cf = np.empty(nr), np.empty(q * nr)
+    call('sclbm_noise_operator', ctypes.byref(p), float(kBT), float(n0), ptr(mv), ptr(cf))
+    return mv, cf.reshape(q, nr)

@@ -35,6 +35,10 @@
  *                                           idpy/LBM/LBMKernelsMeta.py:389-498
  *   sclbm_center_of_mass    ComputeCenterOfMass  idpy/LBM/MultiPhase.py:108-137
  *   sclbm_density_at        K_NInNOut (used by DeltaPLaplace) idpy/LBM/LBMKernels.py:506-523
+ *   sclbm_set_fluctuations  ShanChenMultiPhase(fluctuations='Gross2011', ...) + CRNGS +
+ *                           MainLoopGross2011SRT idpy/LBM/MultiPhase.py:1404-1541,2029-2069,
+ *                                           idpy/PRNGS/CRNGS.py:87-337
+ *   sclbm_get_seeds         crng.sims_idpy_memory['seeds'].D2H()
  *   sclbm_destroy           End()            idpy/LBM/MultiPhase.py:2171-2175
  */
 #ifndef SCLBM_H
@@ -156,6 +160,43 @@ SCLBM_API int sclbm_init_cylinder(sclbm_sim *s, double n_g, double n_l, double R
  * population pushed into a wall returns to the opposite population of its own
  * cell (halfway bounce-back); the two-pass kernels run (no single pass). */
 SCLBM_API int sclbm_set_walls(sclbm_sim *s, const int *walls, const double *psi);
+
+/* fluctuations: the Gross et al. (2011) fluctuating step
+ * (MainLoopGross2011SRT, idpy/LBM/MultiPhase.py:1404-1541; its kernel
+ * K_ForceGross2011CollideStreamSCMPMeta, idpy/LBM/MultiPhaseKernelsMeta.py:1369-1557;
+ * generators and Box-Muller, idpy/PRNGS/CRNGS.py:603-1276).  Every step adds to
+ * population q the noise sum_k coef[q*nr+k] Rm_k (in the reference's print order,
+ * the moment names Rm_0, Rm_1, Rm_10, ... sorted as strings), where the nr = q-dim-1
+ * random moments are Rm_k = sqrt(m2var[k] log(u0)) cos(2 pi u1), u0, u1 uniform from
+ * the cell's congruential generators: generator k drawn twice (indep = 0), or
+ * generators 2k and 2k+1 drawn once each (indep = 1, the reference's
+ * indep_gaussian).  BGK collision only; not with walls; the two-pass kernels run. */
+#define SCLBM_CRNG_NONE   0   /* fluctuations off */
+#define SCLBM_CRNG_MINSTD 1   /* Park-Miller 16807 mod 2^31-1 (64-bit product form), uint32 states */
+#define SCLBM_CRNG_NUMREC 2   /* x*1664525 + 1013904223 mod 2^32, uint32 states */
+#define SCLBM_CRNG_MMIX   3   /* x*6364136223846793005 + 1442695040888963407 mod 2^64, uint64 states */
+/* layout of the generator states: seeds[s*V + g] (the reference's 'gpu'
+ * ordering, MultiPhase.py:1962-1963) or seeds[s + g*streams] (its 'cpu' one) */
+#define SCLBM_SEEDS_STREAM_MAJOR 0
+#define SCLBM_SEEDS_CELL_MAJOR   1
+
+/* random moments (q - dim - 1) and generator states per cell (nr or 2 nr) */
+SCLBM_API int sclbm_noise_counts(int dim, int q, int indep, int *moments, int *streams);
+/* host only: the noise operator GrossShanChenMultiPhase builds
+ * (idpy/LBM/Fluctuations.py:40-165) for the lattice, tau and literal mode of p:
+ * m2var[nr] = -2 var_k, var_k = norm_k kBT (2 - 1/tau)/tau/c2 n0, and
+ * coef[q*nr] = Mw^-1[q][dim+1+k] (Mw the W-orthogonal Hermite basis) */
+SCLBM_API int sclbm_noise_operator(const sclbm_params *p, double kBT, double n0, double *m2var, double *coef);
+/* switch the fluctuations on (generator SCLBM_CRNG_*) or off (SCLBM_CRNG_NONE).
+ * seeds: V * streams initial states (uint32, or uint64 for MMIX) in the given
+ * layout.  m2var / coef: null to build the operator from kBT, n0 and the current
+ * BGK tau, or the operator to use (e.g. a generated reference kernel's
+ * literals).  The operator is kept across sclbm_set_collision; call again after
+ * changing tau. */
+SCLBM_API int sclbm_set_fluctuations(sclbm_sim *s, int generator, int indep, double kBT, double n0,
+                                     const void *seeds, int layout, const double *m2var, const double *coef);
+/* the current generator states (crng.sims_idpy_memory['seeds'].D2H()) */
+SCLBM_API int sclbm_get_seeds(sclbm_sim *s, void *seeds, int layout);
 
 /* time stepping: enqueue nsteps steps on the handle's stream (returns without
  * waiting); sclbm_sync waits for everything enqueued on the handle */

@@ -25,6 +25,9 @@ What is restated where:
   * initial profiles: idpy/LBM/MultiPhaseKernels.py:44-112,605-777
   * CheckUConvergenceSCMP: idpy/LBM/MultiPhaseLoopChecks.py:96-163
   * DeltaPLaplace / PBulk / ComputeCenterOfMass: idpy/LBM/MultiPhase.py:108-137,1690-1768
+  * Gross et al. (2011) fluctuations: ``noise_terms``, ``noise_variance``,
+    ``OracleSim.set_fluctuations``  idpy/LBM/Fluctuations.py:40-165,
+    idpy/PRNGS/CRNGS.py:603-1276, idpy/LBM/MultiPhaseKernelsMeta.py:1369-1557
 """
 import ctypes
 import math
@@ -311,6 +314,56 @@ def mrt_terms(xi, w, c2, rates, mode='round15'):
     return out
 
 
+CRNG_KINDS = {'MINSTD': 1, 'NUMREC': 2, 'MMIX': 3}
+
+
+def noise_variance(norm, kBT, tau, n0, c2=1.0 / 3.0):
+    """Variance literal of one random moment, as GetVariances evaluates and
+    prints it (idpy/LBM/Fluctuations.py:72-97): norm * kBT * (2 - 1/tau) / tau
+    / c_s2 * n0, each product and quotient rounded to double (sympy Float at
+    53 bits), printed with 15 significant digits.  tau is 1/OMEGA as the
+    kernel passes it (MultiPhaseKernelsMeta.py:1521)."""
+    a = float(Fraction(norm)) * kBT
+    a = a * (2 - 1 / tau)
+    a = a / tau
+    a = a / c2
+    a = a * n0
+    return round15(a)
+
+
+def noise_terms(xi, w, c2, mode='round15'):
+    """Noise populations rpop = Mw^-1 [0 .. 0, Rm_0 .. Rm_{Q-D-2}]
+    (Fluctuations.py:158-163) as exact coefficients of the random moments, per
+    population a list of (literal, moment) in sympy's print order (the moment
+    names sorted as strings: Rm_0, Rm_1, Rm_10, ..., Rm_2, ...), and the
+    Hermite norms sum_q w_q Mw[k][q]^2 of the random moments
+    (IdpyStencils.py:977-980)."""
+    Q, D = len(xi), len(xi[0])
+    _, Mw = hermite_bases(xi, w, c2)
+    Mwi = _inverse(Mw)
+    W = [Fraction(x).limit_denominator(10000) for x in w]
+    norms = [sum(W[q] * Mw[k][q] * Mw[k][q] for q in range(Q)) for k in range(D + 1, Q)]
+    nr = Q - (D + 1)
+    order = sorted(range(nr), key=lambda j: 'Rm_%d' % j)
+    out = []
+    for q in range(Q):
+        tl = []
+        for j in order:
+            c = Mwi[q][D + 1 + j]
+            if c == 0:
+                continue
+            tl.append((round15(c) if mode == 'round15' else float(c), j))
+        out.append(tl)
+    return out, norms
+
+
+def noise_from_literals(noise):
+    """(terms, m2var) straight from the reference's generated literals
+    (fixture dict with 'var' and 'terms')."""
+    terms = [[(float(c), int(k)) for k, c in tl] for tl in noise['terms']]
+    return terms, [-2.0 * float(v) for v in noise['var']]
+
+
 def terms_from_literals(lit):
     """Terms straight from the reference's generated literals (fixture dict)."""
     out = []
@@ -332,6 +385,12 @@ class _Cfg(ctypes.Structure):
                 ('t_nf', ctypes.c_void_p), ('t_fid', ctypes.c_void_p),
                 ('v_off', ctypes.c_void_p), ('v_pop', ctypes.c_void_p),
                 ('v_sign', ctypes.c_void_p), ('n_order', ctypes.c_void_p)]
+
+
+class _Noise(ctypes.Structure):
+    _fields_ = [('kind', ctypes.c_int), ('indep', ctypes.c_int), ('nr', ctypes.c_int),
+                ('m2var', ctypes.c_void_p), ('t_off', ctypes.c_void_p), ('t_mom', ctypes.c_void_p),
+                ('t_coef', ctypes.c_void_p)]
 
 
 def _ptr(a):
@@ -437,9 +496,54 @@ class OracleSim:
         opp = [self.xi.index(tuple(-v for v in x)) for x in self.xi]
         self.opposite = np.array(opp, np.int32)
 
+    def set_fluctuations(self, kind, indep, kBT, n0, seeds, tau, noise_literals=None, mode='round15'):
+        """Gross et al. (2011) fluctuations (MainLoopGross2011SRT,
+        idpy/LBM/MultiPhase.py:1404-1541): generator kind ('MINSTD', 'NUMREC',
+        'MMIX'), one (indep False) or two (True) streams per random moment,
+        seeds in the reference's CPU ordering (stream + cell * streams).  The
+        noise operator comes from noise_terms (exact, 15-digit literals) or
+        from the reference's own literals."""
+        D, Q = self.D, self.Q
+        nr = Q - (D + 1)
+        if noise_literals is not None:
+            terms, m2var = noise_from_literals(noise_literals)
+        else:
+            terms, norms = noise_terms(self.xi, self.w, self.c2, mode)
+            omega = 1.0 / tau
+            m2var = [-2.0 * noise_variance(nm, kBT, 1.0 / omega, n0) for nm in norms]
+        self.noise_terms, self.noise_m2var = terms, m2var
+        off, mom, coef = [0], [], []
+        for tl in terms:
+            for c, j in tl:
+                coef.append(c)
+                mom.append(j)
+            off.append(len(coef))
+        self._z_off = np.array(off, np.int32)
+        self._z_mom = np.array(mom, np.int32)
+        self._z_coef = np.array(coef, np.float64)
+        self._z_m2var = np.array(m2var, np.float64)
+        ns = 2 * nr if indep else nr
+        seeds = np.asarray(seeds)
+        if seeds.size != ns * self.V:
+            raise ValueError('expected %d generator states' % (ns * self.V))
+        self.seeds = np.ascontiguousarray(seeds.astype(np.uint64).ravel())
+        self.seeds_dtype = seeds.dtype
+        z = _Noise()
+        z.kind, z.indep, z.nr = CRNG_KINDS[kind], int(bool(indep)), nr
+        z.m2var, z.t_off, z.t_mom, z.t_coef = _ptr(self._z_m2var), _ptr(self._z_off), _ptr(self._z_mom), \
+            _ptr(self._z_coef)
+        self.noise = z
+
+    def get_seeds(self):
+        """Generator states in the reference's CPU ordering and dtype."""
+        return self.seeds.astype(self.seeds_dtype)
+
     def run(self, nsteps):
         sw = ctypes.c_int(0)
-        if getattr(self, 'walls', None) is not None:
+        if getattr(self, 'noise', None) is not None:
+            lib().orc_run_noise(ctypes.byref(self.cfg), ctypes.byref(self.noise), _ptr(self.pop), _ptr(self.pop_swap),
+                                _ptr(self.n), _ptr(self.psi_arr), _ptr(self.seeds), int(nsteps), ctypes.byref(sw))
+        elif getattr(self, 'walls', None) is not None:
             # MainLoopWalls (idpy/LBM/MultiPhase.py:1226-1309)
             lib().orc_run_walls(ctypes.byref(self.cfg), _ptr(self.pop), _ptr(self.pop_swap), _ptr(self.n),
                                 _ptr(self.psi_arr), _ptr(self.walls), _ptr(self.opposite), int(nsteps),

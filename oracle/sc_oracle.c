@@ -311,3 +311,99 @@ int orc_run_walls(const orc_cfg *c, double *pop_a, double *pop_b, double *n, dou
     *swapped = (cur != pop_a);
     return 0;
 }
+
+/* ---- fluctuations (Gross et al. 2011, MainLoopGross2011SRT, idpy/LBM/MultiPhase.py:1404-1541) ----
+ * K_ForceGross2011CollideStreamSCMPMeta (idpy/LBM/MultiPhaseKernelsMeta.py:1369-1557) is the
+ * BGK + Guo push step with, for every population q, the terms coef * Rm_k added one by one
+ * after the collided value (Collisions.py:526-527), where Rm_k are Gaussian random moments:
+ *   Rm_k = sqrt(-2 var_k log(u0)) cos(TWOPI u1) + 0        (CRNGS.py:924-1058)
+ * u0, u1 uniform in [0, 1] from congruential generators (CRNGS.py:603-735): one stream per
+ * moment drawn twice, or (independent mode) streams 2k and 2k+1 drawn once each.  Generator
+ * states are read at the start of the cell update and written back at its end
+ * (CRNGS.py:1061-1113).  seeds[s + g * ns], the reference's CPU ordering
+ * (MultiPhase.py:1964-1965); 32-bit generators keep their state in the low 32 bits. */
+enum { ORC_CRNG_MINSTD = 1, ORC_CRNG_NUMREC = 2, ORC_CRNG_MMIX = 3 };
+
+typedef struct {
+    int kind;              /* ORC_CRNG_* */
+    int indep;             /* 0: one stream per moment, 1: two */
+    int nr;                /* random moments, Q - (D + 1) */
+    const double *m2var;   /* nr: -2 * variance (the product the generated C folds) */
+    const int *t_off;      /* Q+1: noise terms of population q in [t_off[q], t_off[q+1]) */
+    const int *t_mom;      /* moment of each term */
+    const double *t_coef;  /* literal of each term */
+} orc_noise;
+
+static const double ORC_TWOPI = 6.283185307179586;  /* 2. * np.pi, the reference's TWOPI */
+
+/* one step of the generator (MMIX CRNGS.py:717-731, NUMREC :705-715, MINSTD 64-bit :674-703) */
+static inline uint64_t crng_next(int kind, uint64_t s) {
+    if (kind == ORC_CRNG_MMIX) return s * 6364136223846793005ULL + 1442695040888963407ULL;
+    if (kind == ORC_CRNG_NUMREC) return (uint32_t)((uint32_t)s * 1664525U + 1013904223U);
+    const uint64_t sw = 16807ULL * (uint32_t)s;
+    uint32_t r = (uint32_t)((sw & 0x7fffffffULL) + (sw >> 31));
+    if (r & 0x80000000U) r = (r & 0x7fffffffU) + 1U;
+    return r;
+}
+
+/* ((PopType)seed) / ((PopType)ID_RANDMAX_<kind>)  (CRNGS.py:737-773) */
+static inline double crng_flat(int kind, uint64_t s) {
+    if (kind == ORC_CRNG_MMIX) return (double)s / 18446744073709551616.0;  /* (double)(2^64 - 1) */
+    if (kind == ORC_CRNG_NUMREC) return (double)(uint32_t)s / 4294967295.0;
+    return (double)(uint32_t)s / 2147483647.0;
+}
+
+int orc_force_collide_stream_noise(const orc_cfg *c, const orc_noise *z, const double *pop, const double *n,
+                                   const double *psi, uint64_t *seeds, double *pop_swap) {
+    const long V = volume(c);
+    const int Q = c->Q, D = c->dim, ns = z->indep ? 2 * z->nr : z->nr;
+    double v[1 + 6 + ORC_MAXQ];
+    double rm[ORC_MAXQ];
+    for (long g = 0; g < V; g++) {
+        int x[3];
+        coords(c, g, x);
+        double F[3];
+        sc_force(c, psi, g, x, F);
+        const double *f = pop + g * Q;
+        double u[3];
+        velocity(c, f, n[g], F, u);
+        uint64_t *sd = seeds + g * ns;
+        for (int k = 0; k < z->nr; k++) {
+            double u0, u1;
+            if (z->indep) {
+                sd[2 * k] = crng_next(z->kind, sd[2 * k]);
+                u0 = crng_flat(z->kind, sd[2 * k]);
+                sd[2 * k + 1] = crng_next(z->kind, sd[2 * k + 1]);
+                u1 = crng_flat(z->kind, sd[2 * k + 1]);
+            } else {
+                sd[k] = crng_next(z->kind, sd[k]);
+                u0 = crng_flat(z->kind, sd[k]);
+                sd[k] = crng_next(z->kind, sd[k]);
+                u1 = crng_flat(z->kind, sd[k]);
+            }
+            rm[k] = sqrt(z->m2var[k] * log(u0)) * cos(ORC_TWOPI * u1) + 0.;
+        }
+        v[0] = n[g];
+        for (int d = 0; d < D; d++) { v[1 + d] = u[d]; v[1 + D + d] = F[d]; }
+        for (int q = 0; q < Q; q++) v[1 + 2 * D + q] = f[q];
+        for (int q = 0; q < Q; q++) {
+            const long dst = neighbour(c, x, c->xi + q * D);
+            double acc = eval_terms(c, q, v);
+            for (int t = z->t_off[q]; t < z->t_off[q + 1]; t++) acc = acc + z->t_coef[t] * rm[z->t_mom[t]];
+            pop_swap[q + dst * Q] = acc;
+        }
+    }
+    return 0;
+}
+
+int orc_run_noise(const orc_cfg *c, const orc_noise *z, double *pop_a, double *pop_b, double *n, double *psi,
+                  uint64_t *seeds, int nsteps, int *swapped) {
+    double *cur = pop_a, *nxt = pop_b;
+    for (int s = 0; s < nsteps; s++) {
+        orc_density_psi(c, cur, n, psi);
+        orc_force_collide_stream_noise(c, z, cur, n, psi, seeds, nxt);
+        double *t = cur; cur = nxt; nxt = t;
+    }
+    *swapped = (cur != pop_a);
+    return 0;
+}

@@ -1,0 +1,158 @@
+"""Fluctuating Shan-Chen step on the GPU (sclbm_set_fluctuations, the drop-in
+MainLoopGross2011SRT) against the reference's own runs
+(tests/golden/gross_*.npz):
+
+* generator states bit-identical to the reference after every recorded step
+  count (integer recurrences);
+* FP64 populations within 1e-12 (relative, max-norm) of the reference: the
+  Box-Muller uses CUDA's log and cos, which may differ from glibc's by an ulp;
+* the same through the drop-in class with the reference's seeding and CPU
+  ordering;
+* at sizes beyond the fixtures, equipartition of the ideal gas (G = 0):
+  <n u_a^2> = kBT and <dn^2> c_s^2 / n0 = kBT within 5 %, FP64 and FP32, in
+  2D and 3D; mass conserved by the noise.
+"""
+import numpy as np
+import pytest
+
+from helpers import rel_err
+from sclbm import _lib, XIStencils, FStencils
+from sclbm.MultiPhase import ShanChenMultiPhase
+from test_gross import CASES, load
+
+pytestmark = pytest.mark.gpu
+
+
+def ref_tables(nl, Q, D):
+    nr = Q - D - 1
+    coef = np.zeros((Q, nr))
+    for q, tl in enumerate(nl['terms']):
+        for k, lit in tl:
+            coef[q, int(k)] = float(lit)
+    return np.array([-2.0 * float(v) for v in nl['var']]), coef
+
+
+def start(z, c, nl=None, **kw):
+    x, f = XIStencils[c['xi']], FStencils[c['fs']]
+    D = len(c['dims'])
+    psi = _lib.PSI_EXP_INV if c['psi'] == 'exp' else _lib.PSI_ONE_MINUS_EXP
+    s = _lib.Sim(D, c['dims'], x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], c['G'], psi_kind=psi, tau=c['tau'],
+                 **kw)
+    s.set_density(z['n_init'])
+    s.set_velocity(np.zeros(D * s.V))
+    s.init_populations()
+    mv = cf = None
+    if nl is not None:
+        mv, cf = ref_tables(nl, len(x['XIs']), D)
+    s.set_fluctuations(c['kind'], c['indep'], c['kBT'], c['n0'], z['seeds_init'], _lib.SEEDS_CELL_MAJOR, mv, cf)
+    return s
+
+
+@pytest.mark.parametrize('own', [False, True])
+@pytest.mark.parametrize('name', CASES)
+def test_fluctuating_step_matches_reference(name, own):
+    z, c, nl = load(name)
+    s = start(z, c, None if own else nl)
+    assert s.kernels_per_step() == 2
+    Q = z['pop_init'].shape[0]
+    done = 0
+    for k in z['steps']:
+        s.step(int(k) - done)
+        done = int(k)
+        assert np.array_equal(s.get_seeds(_lib.SEEDS_CELL_MAJOR), z['seeds_%d' % k]), (name, k)
+        got = s.get_populations().reshape(Q, -1)
+        want = z['pop_%d' % k].reshape(Q, -1)
+        assert rel_err(got, want) < 1e-12, (name, own, k, rel_err(got, want))
+    s.close()
+
+
+@pytest.mark.parametrize('name', ['d2e4_mmix_t1', 'd3e6_minstd_indep_t09'])
+def test_dropin_gross_loop_matches_reference(name):
+    """ShanChenMultiPhase(fluctuations='Gross2011', ...) seeded like the
+    reference, CPU ordering, MainLoopGross2011SRT in the fixture's chunks."""
+    sp = pytest.importorskip('sympy')
+    z, c, _ = load(name)
+    n = sp.Symbol('n')
+    sc = ShanChenMultiPhase(lang='cuda', dim_sizes=tuple(c['dims']), xi_stencil=XIStencils[c['xi']],
+                            f_stencil=FStencils[c['fs']], psi_code='exp(-1./ln_0)', psi_sym=sp.exp(-1 / n),
+                            SC_G=c['G'], tau=c['tau'], fluctuations='Gross2011', prng_kind=c['kind'],
+                            init_seed=c['init_seed'], prng_init_from='numpy', prng_distribution='gaussian',
+                            indep_gaussian=c['indep'], set_ordering='cpu')
+    sc.verbose = False
+    assert np.array_equal(sc.crng.sims_idpy_memory['seeds'].D2H(), z['seeds_init'])
+    sc.sims_idpy_memory['n'].H2D(z['n_init'].ravel())
+    sc.sims_idpy_memory['u'].SetConst(0.0)
+    sc.init_status['n'] = sc.init_status['u'] = True
+    sc.InitPopulations()
+    Q = z['pop_init'].shape[0]
+    done = 0
+    for k in z['steps']:
+        sc.MainLoopGross2011SRT([0, int(k) - done], kBT=c['kBT'], n0=c['n0'], print_flag=False)
+        done = int(k)
+        pop = sc.GetPopulations()   # cpu ordering: (*flip(dims), Q)
+        want = np.moveaxis(z['pop_%d' % k], 0, -1)
+        assert rel_err(pop, want) < 1e-12, (name, k)
+        assert np.array_equal(sc.crng.sims_idpy_memory['seeds'].D2H(), z['seeds_%d' % k])
+    # a deterministic loop afterwards keeps the generator states
+    sc.MainLoop([0, 3])
+    assert np.array_equal(sc.crng.sims_idpy_memory['seeds'].D2H(), z['seeds_%d' % z['steps'][-1]])
+    sc.End()
+
+
+def equipartition(lat, dims, precision, kind, indep, steps_eq, samples, every, kBT=1e-4, n0=1.0, tau=1.0):
+    x = XIStencils[lat]
+    f = FStencils['D2E4' if lat == 'D2Q9' else 'D3E4']
+    D = len(dims)
+    s = _lib.Sim(D, dims, x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], 0.0, psi_kind=_lib.PSI_IDENTITY, tau=tau,
+                 precision=precision, rho0=n0)
+    s.set_density(np.full(s.V, n0))
+    s.set_velocity(np.zeros(D * s.V))
+    s.init_populations()
+    nr, ns = _lib.noise_counts(D, len(x['Ws']), indep)
+    rng = np.random.default_rng(5)
+    hi = 2 ** 63 if kind == 'MMIX' else 2 ** 31 - 2
+    dt = np.uint64 if kind == 'MMIX' else np.uint32
+    seeds = rng.integers(1, hi, ns * s.V, dtype=np.int64).astype(dt)
+    s.set_fluctuations(kind, indep, kBT, n0, seeds, _lib.SEEDS_STREAM_MAJOR)
+    m0, _ = s.reductions()
+    s.step(steps_eq)
+    ju, dn = [], []
+    for _ in range(samples):
+        s.step(every)
+        s.compute_moments()
+        n = s.get_density()
+        u = s.get_velocity().reshape(D, -1)
+        ju.append(np.mean(n * u * u) * 1.0)
+        dn.append(np.mean((n - n.mean()) ** 2))
+    m1, _ = s.reductions()
+    s.close()
+    return np.mean(ju) / kBT, np.mean(dn) * x['c2'] / (n0 * kBT), abs(m1 - m0) / m0
+
+
+@pytest.mark.parametrize('lat,dims,precision,kind,indep', [
+    ('D2Q9', (128, 128), _lib.FP64, 'MMIX', False),
+    ('D2Q9', (128, 128), _lib.FP32_SHIFTED, 'MINSTD', True),
+    ('D3Q19', (48, 48, 48), _lib.FP64, 'NUMREC', False),
+    ('D3Q19', (48, 48, 48), _lib.FP32_SHIFTED, 'MMIX', False),
+])
+def test_equipartition_ideal_gas(lat, dims, precision, kind, indep):
+    """G = 0: every velocity component carries kBT / n0 and the density
+    fluctuations n0 kBT / c_s^2 (fluctuation-dissipation of the noise
+    variances norm_k kBT (2 - 1/tau)/tau / c_s^2 n0)."""
+    ju, dn, dm = equipartition(lat, dims, precision, kind, indep, 2000, 40, 25)
+    assert abs(ju - 1.0) < 0.05, ju
+    assert abs(dn - 1.0) < 0.05, dn
+    assert dm < (1e-12 if precision == _lib.FP64 else 1e-4), dm
+
+
+def test_fluctuations_refused_with_mrt_and_walls():
+    z, c, nl = load('d2e4_mmix_t1')
+    s = start(z, c, nl)
+    with pytest.raises(_lib.SclbmError):
+        s.set_collision(_lib.COLL_MRT, mrt_s=np.diag(np.linspace(1.0, 1.4, 9)))
+    with pytest.raises(_lib.SclbmError):
+        s.set_walls(np.ones(s.V, np.int32), np.zeros(s.V))
+    s.set_fluctuations(None, False, 0, 0, None)
+    s.set_collision(_lib.COLL_MRT, mrt_s=np.diag(np.linspace(1.0, 1.4, 9)))
+    s.step(2)
+    s.close()
