@@ -20,6 +20,7 @@
 #pragma once
 
 #include "kernels.cuh"
+#include "noise.cuh"
 
 namespace sclbm {
 
@@ -40,6 +41,8 @@ struct FusedShape {
     // floats of one plane's staged halo populations (2D only: see k_fused)
     static constexpr int STAGE = D == 2 ? HPT * L::Q * NT : 0;
     static constexpr int SMEM = (RING * HC + 2 * STAGE) * 4;  // psi ring + double-buffered stage
+    // fluctuating step: plus each thread's random moments of its current cell
+    static constexpr int NSMEM = SMEM + (L::Q - D - 1) * NT * 4;
 };
 
 __device__ __forceinline__ void cp_async4(float *smem, const float *gmem) {
@@ -97,11 +100,16 @@ __device__ __forceinline__ float bgk_fp32(const float *f, const float *u, const 
 // One work item: the tile (x0, y0) of one lattice, planes [m0, m1).  pop and
 // pop_out point at the lattice's first cell, V is the distance between two
 // populations of a cell (the lattice volume, or a batch's total volume).
-template <class L, class S, bool MRT>
+// ST (not void): the fluctuating step (noise.cuh), generator states of type ST
+// at seeds[s*V + cell].
+template <class L, class S, bool MRT, class ST = void>
 __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float *__restrict__ pop_out, const int V,
                                            const int Lx, const int Ly, const int Lz, const int x0, const int y0,
                                            const int m0, const int m1, const float neg_g, const float rho0,
-                                           const StepParams<L, S, float> &p, float *smem) {
+                                           const StepParams<L, S, float> &p, float *smem,
+                                           ST *seeds = nullptr, const NoiseParams<L, float> *z = nullptr) {
+    constexpr bool NOISE = !std::is_void<ST>::value;
+    using SeedT = typename std::conditional<NOISE, ST, int>::type;
     using SH = FusedShape<L, S>;
     constexpr int D = L::D, Q = L::Q, R = SH::R, HX = SH::HX, HC = SH::HC, NT = SH::NT, RING = SH::RING;
     float *ring = smem;  // psi ring [RING][HC], then (2D) 2 stage buffers [HPT][Q][NT]
@@ -199,9 +207,14 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
         for (int o = -1; o <= 1; o++) Z3[o + 1] = D == 3 ? wrapc(m + o, Lm) * PL : wrapc(m + o, Lm) * Lx;
         const int g = own + Z3[1];
         float f[Q];
+        constexpr int NR = NoiseParams<L, float>::NR;
+        SeedT st[NOISE ? NR : 1];
         if (in_tile) {
 #pragma unroll
             for (int q = 0; q < Q; q++) f[q] = __ldg(pop + (g + q * V));
+            // generator states with the populations: their loads overlap the psi plane
+            // (one generator per moment: the two-generator mode runs the two-pass kernel)
+            if constexpr (NOISE) noise_load<L, SeedT, int>(0, seeds, (int64_t)V, (int64_t)g, st);
         }
         if (STAGED) {
             if (m + 1 < m1) {
@@ -220,6 +233,16 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
             const float *sb[RING];
 #pragma unroll
             for (int k = 0; k < RING; k++) sb[k] = ring + wrapm(m + k - R, RING) * HC + ty * HX + tx;
+            // random moments of the cell into this thread's shared-memory slot
+            // (the states die here; the collision reads the moments back)
+            float *rms = smem + SH::RING * SH::HC + 2 * SH::STAGE + tid;
+            if constexpr (NOISE) {
+                float rm[NR];
+                noise_compute<L, float, false, SeedT>(*z, 0, st, rm);
+                noise_store<L, SeedT, int>(0, seeds, (int64_t)V, (int64_t)g, st);
+#pragma unroll
+                for (int k = 0; k < NR; k++) rms[k * NT] = rm[k];
+            }
             float d = f[lex_q<Q>(0)];
 #pragma unroll
             for (int i = 1; i < Q; i++) d += f[lex_q<Q>(i)];
@@ -257,6 +280,8 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
                 float out;
                 if (MRT) collide_cell<L, S, true, float, false>(f, d, n, u, F, q, p, out);
                 else out = bgk_fp32<L, S>(f, u, F, q, p, C0, a, b);
+                if constexpr (NOISE)
+                    add_noise_terms_strided<NR, NT>(z->coef[q], rms, out, std::make_integer_sequence<int, NR>{});
                 // __fsub_rn: no contraction with the product that made `out`
                 // (at omega = 1 it is a plain multiply), so the rest population
                 // balances exactly the rounded values that are stored
@@ -270,7 +295,8 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
 }
 
 // Three CTAs per SM for BGK (80 registers, no spills; 5% faster than two at
-// 256^3 D3Q19 E6, measured in one run), two for the dense MRT operator.
+// 256^3 D3Q19 E6, measured in one run), two for the dense MRT operator and
+// for the fluctuating step.
 template <class L, class S, bool MRT>
 __global__ void __launch_bounds__(FusedShape<L, S>::NT, MRT ? 2 : 3)
     k_fused(const float *__restrict__ pop, float *__restrict__ pop_out, const __grid_constant__ StepParams<L, S, float> p,
@@ -287,6 +313,26 @@ __global__ void __launch_bounds__(FusedShape<L, S>::NT, MRT ? 2 : 3)
         const int m0 = ic * fg.chunk;
         fused_tile<L, S, MRT>(pop, pop_out, (int)fg.V, fg.L[0], fg.L[1], fg.L[2], ix * SH::TX, iy * SH::TY, m0,
                               min(m0 + fg.chunk, Lm), p.neg_g, p.rho0, p, smem);
+    }
+}
+
+template <class L, class S, class ST>
+__global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
+    k_fused_noise(const float *__restrict__ pop, float *__restrict__ pop_out,
+                  const __grid_constant__ StepParams<L, S, float> p, const FusedGeom fg, ST *__restrict__ seeds,
+                  const __grid_constant__ NoiseParams<L, float> z) {
+    using SH = FusedShape<L, S>;
+    constexpr int D = L::D;
+    extern __shared__ float smem[];
+    const int Lm = D == 3 ? fg.L[2] : fg.L[1];
+    for (int item = blockIdx.x; item < fg.items; item += gridDim.x) {
+        const int ix = item % fg.tiles_x;
+        const int rest = item / fg.tiles_x;
+        const int iy = D == 3 ? rest % fg.tiles_y : 0;
+        const int ic = D == 3 ? rest / fg.tiles_y : rest;
+        const int m0 = ic * fg.chunk;
+        fused_tile<L, S, false, ST>(pop, pop_out, (int)fg.V, fg.L[0], fg.L[1], fg.L[2], ix * SH::TX, iy * SH::TY,
+                                    m0, min(m0 + fg.chunk, Lm), p.neg_g, p.rho0, p, smem, seeds, &z);
     }
 }
 

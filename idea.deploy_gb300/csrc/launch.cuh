@@ -76,7 +76,12 @@ struct KernelOps {
     size_t noise_size;
     void (*fill_noise)(void *params, int kind, int indep, const double *m2var, const double *coef);
     cudaError_t (*fcs_noise)(const void *pop, void *pop_out, const void *dn, const void *psi, void *seeds,
-                             const void *step_params, const void *noise_params, int sms, cudaStream_t st);
+                             const void *step_params, const void *noise_params, int grid, cudaStream_t st);
+    int (*noise_occupancy)();
+    // single-pass fluctuating step (FP32 BGK only, else null)
+    cudaError_t (*fused_noise)(const void *pop, void *pop_out, const void *step_params, const FusedGeom &fg,
+                               void *seeds, const void *noise_params, int grid, cudaStream_t st);
+    int (*fused_noise_occupancy)();
 };
 
 template <class L, class S, bool MRT, class Real, bool STRICT>
@@ -274,20 +279,68 @@ struct Ops {
             for (int k = 0; k < NP::NR; k++) z->coef[q][k] = (Real)coef[q * NP::NR + k];
     }
     static cudaError_t fcs_noise(const void *pop, void *pop_out, const void *dn, const void *psi, void *seeds,
-                                 const void *sp, const void *np, int sms, cudaStream_t st) {
+                                 const void *sp, const void *np, int grid, cudaStream_t st) {
         if constexpr (!MRT) {
-            static int per_sm = 0;
-            if (!per_sm) {
-                int b = 0;
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fcs_noise<L, S, Real, STRICT>, 128, 0);
-                per_sm = b > 0 ? b : 1;
-            }
-            k_fcs_noise<L, S, Real, STRICT><<<sms * per_sm, 128, 0, st>>>(
-                (const Real *)pop, (Real *)pop_out, (const Real *)dn, (const Real *)psi, seeds,
-                *static_cast<const SP *>(sp), *static_cast<const NP *>(np));
+            const NP &z = *static_cast<const NP *>(np);
+            if (z.kind == CRNG_MMIX)
+                k_fcs_noise<L, S, Real, STRICT, unsigned long long><<<grid, 128, 0, st>>>(
+                    (const Real *)pop, (Real *)pop_out, (const Real *)dn, (const Real *)psi,
+                    (unsigned long long *)seeds, *static_cast<const SP *>(sp), z);
+            else
+                k_fcs_noise<L, S, Real, STRICT, unsigned int><<<grid, 128, 0, st>>>(
+                    (const Real *)pop, (Real *)pop_out, (const Real *)dn, (const Real *)psi, (unsigned int *)seeds,
+                    *static_cast<const SP *>(sp), z);
             return cudaGetLastError();
         }
         return cudaErrorNotSupported;
+    }
+    static cudaError_t fused_noise(const void *pop, void *pop_out, const void *sp, const FusedGeom &fg, void *seeds,
+                                   const void *np, int grid, cudaStream_t st) {
+        if constexpr (std::is_same<Real, float>::value && !MRT) {
+            using SH = FusedShape<L, S>;
+            allow_smem_noise();
+            const NP &z = *static_cast<const NP *>(np);
+            if (z.kind == CRNG_MMIX)
+                k_fused_noise<L, S, unsigned long long><<<grid, SH::NT, SH::NSMEM, st>>>(
+                    (const float *)pop, (float *)pop_out, *static_cast<const SP *>(sp), fg, (unsigned long long *)seeds,
+                    z);
+            else
+                k_fused_noise<L, S, unsigned int><<<grid, SH::NT, SH::NSMEM, st>>>(
+                    (const float *)pop, (float *)pop_out, *static_cast<const SP *>(sp), fg, (unsigned int *)seeds, z);
+            return cudaGetLastError();
+        }
+        return cudaErrorNotSupported;
+    }
+    static void allow_smem_noise() {
+        if constexpr (std::is_same<Real, float>::value && !MRT) {
+            static bool done[64] = {};  // per device
+            int dev = 0;
+            cudaGetDevice(&dev);
+            if (dev < 0 || dev >= 64 || !done[dev]) {
+                cudaFuncSetAttribute(k_fused_noise<L, S, unsigned int>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     FusedShape<L, S>::NSMEM);
+                cudaFuncSetAttribute(k_fused_noise<L, S, unsigned long long>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, FusedShape<L, S>::NSMEM);
+                if (dev >= 0 && dev < 64) done[dev] = true;
+            }
+        }
+    }
+    static int fused_noise_occupancy() {
+        int b = 0;
+        if constexpr (std::is_same<Real, float>::value && !MRT) {
+            using SH = FusedShape<L, S>;
+            allow_smem_noise();
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fused_noise<L, S, unsigned long long>, SH::NT,
+                                                          SH::NSMEM);
+        }
+        return b > 0 ? b : 1;
+    }
+    static int noise_occupancy() {
+        int b = 0;
+        if constexpr (!MRT)
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fcs_noise<L, S, Real, STRICT, unsigned long long>, 128,
+                                                          0);
+        return b > 0 ? b : 1;
     }
     static const KernelOps *ops() {
         constexpr bool f32 = std::is_same<Real, float>::value;
@@ -299,7 +352,9 @@ struct Ops {
                                     f32 ? &batch_step : nullptr, f32 ? &batch_density : nullptr,
                                     f32 ? &batch_moments : nullptr, f32 ? &batch_mass : nullptr,
                                     f32 ? &batch_add_rest : nullptr, f32 ? &batch_probe : nullptr,
-                                    sizeof(NP), MRT ? nullptr : &fill_noise, MRT ? nullptr : &fcs_noise};
+                                    sizeof(NP), MRT ? nullptr : &fill_noise, MRT ? nullptr : &fcs_noise,
+                                    &noise_occupancy, (f32 && !MRT) ? &fused_noise : nullptr,
+                                    &fused_noise_occupancy};
         return &o;
     }
 };

@@ -96,7 +96,10 @@ __device__ __forceinline__ Real crng_uniform(int kind, uint64_t s) {
     }
 }
 
-// sqrt(-2 var log(u0)) * cos(2 pi u1) + 0, TWOPI = 6.283185307179586 as the reference defines it
+// sqrt(-2 var log(u0)) * cos(2 pi u1) + 0, TWOPI = 6.283185307179586 as the reference defines it.
+// FP32 (a statistical path, not a parity one): the SFU's approximate log2,
+// square root and cosine (relative errors ~1e-7..1e-6, far below the FP32
+// storage noise), the cosine taken on [-pi, pi) as -cos(2 pi (u1 - 1/2)).
 template <class Real, bool STRICT>
 __device__ __forceinline__ Real box_muller(Real m2var, Real u0, Real u1) {
     if constexpr (std::is_same<Real, double>::value) {
@@ -104,45 +107,78 @@ __device__ __forceinline__ Real box_muller(Real m2var, Real u0, Real u1) {
             return __dadd_rn(__dmul_rn(sqrt(__dmul_rn(m2var, log(u0))), cos(__dmul_rn(6.283185307179586, u1))), 0.0);
         return sqrt(m2var * log(u0)) * cos(6.283185307179586 * u1);
     } else {
-        return sqrtf(m2var * logf(u0)) * cospif(2.0f * u1);
+        float l2, r, c;
+        asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(l2) : "f"(u0));
+        const float x = (m2var * 0.6931471805599453f) * l2;  // m2var ln(u0) >= 0
+        asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+        asm("cos.approx.ftz.f32 %0, %1;" : "=f"(c) : "f"(6.283185307179586f * (u1 - 0.5f)));
+        return -r * c;
     }
 }
 
-// the cell's random moments; advances and stores its generator states
+// A cell's generator states are loaded all at once (one memory latency per
+// cell, issued before the force so that its gathers overlap it), advanced in
+// registers and stored back: st[s] = seeds[s*V + g] for s < NR, or < 2 NR
+// with two generators per moment.
+// I: the offset type (int where streams x V < 2^31, checked on the host)
+template <class L, class T, class I = int64_t>
+__device__ __forceinline__ void noise_load(int indep, const T *__restrict__ seeds, int64_t V, int64_t g, T *st) {
+    constexpr int NR = L::Q - L::D - 1;
+    const T *b = seeds + g;
+    const I v = (I)V;
+#pragma unroll
+    for (int s = 0; s < NR; s++) st[s] = b[s * v];
+    if (indep) {
+#pragma unroll
+        for (int s = NR; s < 2 * NR; s++) st[s] = b[s * v];
+    }
+}
+template <class L, class T, class I = int64_t>
+__device__ __forceinline__ void noise_store(int indep, T *__restrict__ seeds, int64_t V, int64_t g, const T *st) {
+    constexpr int NR = L::Q - L::D - 1;
+    T *b = seeds + g;
+    const I v = (I)V;
+#pragma unroll
+    for (int s = 0; s < NR; s++) b[s * v] = st[s];
+    if (indep) {
+#pragma unroll
+        for (int s = NR; s < 2 * NR; s++) b[s * v] = st[s];
+    }
+}
+
+// u0 = 0 (a generator state of 0: NUMREC reaches it once in 2^32 draws of a
+// stream, MMIX once in 2^64) would make log(u0) infinite and, in the
+// reference, the cell's populations with it; here that draw takes the
+// generator's smallest positive uniform (the value of state 1).  The stored
+// state and every other draw are unchanged.
+template <class T>
+__device__ __forceinline__ T nonzero_state(T a) {
+    return a == 0 ? T(1) : a;
+}
+
+// advance the states and form the random moments
 template <class L, class Real, bool STRICT, class T>
-__device__ __forceinline__ void noise_moments_t(const NoiseParams<L, Real> &z, T *__restrict__ seeds, int64_t V,
-                                                int64_t g, Real *rm) {
+__device__ __forceinline__ void noise_compute(const NoiseParams<L, Real> &z, int indep, T *st, Real *rm) {
     constexpr int NR = NoiseParams<L, Real>::NR;
-    if (z.indep) {
+    if (indep) {
 #pragma unroll
         for (int k = 0; k < NR; k++) {
-            T *pa = seeds + (int64_t)(2 * k) * V + g, *pb = seeds + (int64_t)(2 * k + 1) * V + g;
-            const T a = (T)crng_next(z.kind, *pa), b = (T)crng_next(z.kind, *pb);
-            *pa = a;
-            *pb = b;
-            rm[k] = box_muller<Real, STRICT>(z.m2var[k], crng_uniform<Real, STRICT>(z.kind, a),
+            const T a = (T)crng_next(z.kind, st[2 * k]), b = (T)crng_next(z.kind, st[2 * k + 1]);
+            st[2 * k] = a;
+            st[2 * k + 1] = b;
+            rm[k] = box_muller<Real, STRICT>(z.m2var[k], crng_uniform<Real, STRICT>(z.kind, nonzero_state(a)),
                                              crng_uniform<Real, STRICT>(z.kind, b));
         }
     } else {
 #pragma unroll
         for (int k = 0; k < NR; k++) {
-            T *ps = seeds + (int64_t)k * V + g;
-            const T a = (T)crng_next(z.kind, *ps);
+            const T a = (T)crng_next(z.kind, st[k]);
             const T b = (T)crng_next(z.kind, a);
-            *ps = b;
-            rm[k] = box_muller<Real, STRICT>(z.m2var[k], crng_uniform<Real, STRICT>(z.kind, a),
+            st[k] = b;
+            rm[k] = box_muller<Real, STRICT>(z.m2var[k], crng_uniform<Real, STRICT>(z.kind, nonzero_state(a)),
                                              crng_uniform<Real, STRICT>(z.kind, b));
         }
     }
-}
-
-template <class L, class Real, bool STRICT>
-__device__ __forceinline__ void noise_moments(const NoiseParams<L, Real> &z, void *seeds, int64_t V, int64_t g,
-                                              Real *rm) {
-    if (z.kind == CRNG_MMIX)
-        noise_moments_t<L, Real, STRICT>(z, static_cast<unsigned long long *>(seeds), V, g, rm);
-    else
-        noise_moments_t<L, Real, STRICT>(z, static_cast<unsigned int *>(seeds), V, g, rm);
 }
 
 // out[q] += sum_k coef[q][k] Rm_k, term by term in the reference's print order
@@ -158,6 +194,12 @@ __device__ __forceinline__ void add_noise_terms(const Real *coef, const Real *rm
                                                 std::integer_sequence<int, I...>) {
     (add_noise_term<NR, I, Real, STRICT>(coef, rm, acc), ...);
 }
+// FP32 variant reading the moments from a shared-memory slot, rm[k * STRIDE]
+template <int NR, int STRIDE, int... I>
+__device__ __forceinline__ void add_noise_terms_strided(const float *coef, const float *rm, float &acc,
+                                                        std::integer_sequence<int, I...>) {
+    ((acc = fmaf(coef[name_order<NR>(I)], rm[name_order<NR>(I) * STRIDE], acc)), ...);
+}
 template <class L, class Real, bool STRICT>
 __device__ __forceinline__ void add_noise(const NoiseParams<L, Real> &z, const Real *rm, Real *out) {
     constexpr int NR = NoiseParams<L, Real>::NR;
@@ -166,10 +208,12 @@ __device__ __forceinline__ void add_noise(const NoiseParams<L, Real> &z, const R
         add_noise_terms<NR, Real, STRICT>(z.coef[q], rm, out[q], std::make_integer_sequence<int, NR>{});
 }
 
-template <class L, class S, class Real, bool STRICT>
-__global__ void __launch_bounds__(128) k_fcs_noise(const Real *__restrict__ pop, Real *__restrict__ pop_out,
+// four CTAs of 128 threads per SM (at most 128 registers a thread): the
+// batched generator-state loads would otherwise take the whole register file
+template <class L, class S, class Real, bool STRICT, class T>
+__global__ void __launch_bounds__(128, 4) k_fcs_noise(const Real *__restrict__ pop, Real *__restrict__ pop_out,
                                                   const Real *__restrict__ dn, const Real *__restrict__ psi,
-                                                  void *__restrict__ seeds,
+                                                  T *__restrict__ seeds,
                                                   const __grid_constant__ StepParams<L, S, Real> p,
                                                   const __grid_constant__ NoiseParams<L, Real> z) {
     constexpr int D = L::D, Q = L::Q, NR = NoiseParams<L, Real>::NR;
@@ -180,6 +224,8 @@ __global__ void __launch_bounds__(128) k_fcs_noise(const Real *__restrict__ pop,
         Real f[Q];
 #pragma unroll
         for (int q = 0; q < Q; q++) f[q] = __ldg(pop + (int64_t)q * V + g);
+        T st[2 * NR];
+        noise_load<L, T>(z.indep, seeds, V, g, st);
         const Real d = __ldg(dn + g);
         const Real n = p.rho0 + d;
         Real F[D], u[D];
@@ -188,7 +234,8 @@ __global__ void __launch_bounds__(128) k_fcs_noise(const Real *__restrict__ pop,
 #pragma unroll
         for (int q = 0; q < Q; q++) collide_cell<L, S, false, Real, STRICT>(f, d, n, u, F, q, p, out[q]);
         Real rm[NR];
-        noise_moments<L, Real, STRICT>(z, seeds, V, g, rm);
+        noise_compute<L, Real, STRICT, T>(z, z.indep, st, rm);
+        noise_store<L, T>(z.indep, seeds, V, g, st);
         add_noise<L, Real, STRICT>(z, rm, out);
         if constexpr (std::is_same<Real, float>::value) {
             // FP32 storage: rest population from mass conservation (the noise carries no mass)

@@ -239,6 +239,7 @@ struct sclbm_sim {
     void *seeds = nullptr;
     std::vector<double> noise_m2var, noise_coef;
     std::vector<unsigned char> np;  // noise launch parameter block
+    int ngrid = 0;                  // noise kernel grid (resident CTAs, capped by the cells)
     double tau_bgk = 1.0;           // BGK relaxation time of the current operator
     double *red = nullptr;
     int red_blocks = 0;
@@ -331,7 +332,8 @@ bool fused_fits(const sclbm_sim *s) { return (int64_t)s->Q * s->V < ((int64_t)1 
 
 bool fused_path(const sclbm_sim *s) {
     return s->ops->fused != nullptr && s->path != SCLBM_PATH_TWO_PASS && fused_fits(s) && !s->walls &&
-           !s->noise_kind;
+           (!s->noise_kind || (s->ops->fused_noise != nullptr && !s->noise_indep &&
+                               (int64_t)s->noise_streams * s->V < ((int64_t)1 << 31)));
 }
 
 // density + psi of the current populations (fluid cells only with walls)
@@ -346,14 +348,18 @@ int launch_step(sclbm_sim *s, cudaEvent_t *ev = nullptr) {
     const KernelOps *o = s->ops;
     cudaError_t e;
     if (fused_path(s)) {
-        e = o->fused(s->pop[s->cur], s->pop[s->cur ^ 1], s->sp.data(), s->fg, s->fused_grid, s->st);
+        if (s->noise_kind)
+            e = o->fused_noise(s->pop[s->cur], s->pop[s->cur ^ 1], s->sp.data(), s->fg, s->seeds, s->np.data(),
+                               s->fused_grid, s->st);
+        else
+            e = o->fused(s->pop[s->cur], s->pop[s->cur ^ 1], s->sp.data(), s->fg, s->fused_grid, s->st);
         if (ev && e == cudaSuccess) e = cudaEventRecord(ev[0], s->st);
     } else {
         e = density_pass(s);
         if (ev && e == cudaSuccess) e = cudaEventRecord(ev[0], s->st);
         if (e == cudaSuccess && s->noise_kind)
             e = o->fcs_noise(s->pop[s->cur], s->pop[s->cur ^ 1], s->dn, s->psi, s->seeds, s->sp.data(), s->np.data(),
-                             s->sms, s->st);
+                             s->ngrid, s->st);
         else if (e == cudaSuccess && s->walls)
             e = o->fcs_walls(s->pop[s->cur], s->pop[s->cur ^ 1], s->dn, s->psi, s->walls, s->sp.data(), s->fgrid,
                              s->st);
@@ -378,7 +384,7 @@ void plan_fused(sclbm_sim *s) {
     g.tiles_x = (s->L[0] + o->fused_tx - 1) / o->fused_tx;
     g.tiles_y = s->D == 3 ? (s->L[1] + o->fused_ty - 1) / o->fused_ty : 1;
     const int Lm = s->D == 3 ? s->L[2] : s->L[1];
-    const int resident = s->sms * o->fused_occupancy();
+    const int resident = s->sms * (s->noise_kind ? o->fused_noise_occupancy() : o->fused_occupancy());
     const int base = g.tiles_x * g.tiles_y;
     int best_c = 1;
     double best = -1;
@@ -627,6 +633,8 @@ int configure(sclbm_sim *s, int collision, double tau, const double *mrt_s, cons
     if (s->noise_kind) {
         s->np.assign(ops->noise_size, 0);
         ops->fill_noise(s->np.data(), s->noise_kind, s->noise_indep, s->noise_m2var.data(), s->noise_coef.data());
+        s->ngrid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)s->sms * ops->noise_occupancy(),
+                                                               (s->V + 127) / 128));
     }
     ops->grids(s->sms, &s->dgrid, &s->fgrid);
     const int64_t need_d = (s->V + 255) / 256, need_f = (s->V + 127) / 128;
@@ -1138,6 +1146,7 @@ int sclbm_set_fluctuations(sclbm_sim *s, int generator, int indep, double kBT, d
                                                              (s->noise_kind == SCLBM_CRNG_MMIX ? 8 : 4);
         s->seeds = nullptr;
         s->noise_kind = s->noise_streams = 0;
+        plan_fused(s);
         return SCLBM_OK;
     }
     if (generator != SCLBM_CRNG_MINSTD && generator != SCLBM_CRNG_NUMREC && generator != SCLBM_CRNG_MMIX)
@@ -1196,6 +1205,9 @@ int sclbm_set_fluctuations(sclbm_sim *s, int generator, int indep, double kBT, d
     s->noise_coef = cf;
     s->np.assign(s->ops->noise_size, 0);
     s->ops->fill_noise(s->np.data(), s->noise_kind, s->noise_indep, mv.data(), cf.data());
+    s->ngrid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)s->sms * s->ops->noise_occupancy(),
+                                                           (s->V + 127) / 128));
+    plan_fused(s);  // the fluctuating single-pass kernel has its own occupancy
     return SCLBM_OK;
 }
 

@@ -142,7 +142,42 @@ def test_equipartition_ideal_gas(lat, dims, precision, kind, indep):
     ju, dn, dm = equipartition(lat, dims, precision, kind, indep, 2000, 40, 25)
     assert abs(ju - 1.0) < 0.05, ju
     assert abs(dn - 1.0) < 0.05, dn
-    assert dm < (1e-12 if precision == _lib.FP64 else 1e-4), dm
+    # the 15-digit noise literals sum to zero only to ~1e-16 per column: FP64
+    # mass random-walks by ~1e-12 over the 3000 steps
+    assert dm < (1e-10 if precision == _lib.FP64 else 1e-4), dm
+
+
+@pytest.mark.parametrize('lat,kind,indep', [('D2Q9', 'MINSTD', False), ('D3Q19', 'MMIX', False),
+                                            ('D3Q19', 'NUMREC', True)])
+def test_fp32_single_pass_equals_two_pass(lat, kind, indep):
+    """The FP32 fluctuating step in one pass (k_fused_noise) and in two
+    (k_fcs_noise): identical generator states, populations within FP32
+    rounding of the two collision forms.  Two generators per moment always
+    run the two-pass kernels."""
+    x = XIStencils[lat]
+    f = FStencils['D2E6' if lat == 'D2Q9' else 'D3E6']
+    dims = (96, 80) if lat == 'D2Q9' else (40, 36, 32)
+    D = len(dims)
+    from sclbm.profiles import droplet
+    n_init = droplet(dims, 12.0 if D == 2 else 8.0, 4.5625, 0.2086, 2.0, 3)
+    nr, ns = _lib.noise_counts(D, len(x['Ws']), indep)
+    dt = np.uint64 if kind == 'MMIX' else np.uint32
+    seeds = np.random.default_rng(9).integers(1, 2 ** 31 - 2, ns * n_init.size, dtype=np.int64).astype(dt)
+    out = []
+    for path in (_lib.PATH_FUSED, _lib.PATH_TWO_PASS):
+        s = _lib.Sim(D, dims, x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], -4.5, precision=_lib.FP32_SHIFTED,
+                     rho0=0.2086)
+        s.set_density(n_init)
+        s.set_velocity(np.zeros(D * s.V))
+        s.init_populations()
+        s.set_tuning(path)
+        s.set_fluctuations(kind, indep, 1e-5, 1.0, seeds)
+        assert s.kernels_per_step() == (1 if path == _lib.PATH_FUSED and not indep else 2)
+        s.step(50)
+        out.append((s.get_populations(), s.get_seeds()))
+        s.close()
+    assert np.array_equal(out[0][1], out[1][1])
+    assert rel_err(out[0][0], out[1][0]) < 1e-5, rel_err(out[0][0], out[1][0])
 
 
 def test_fluctuations_refused_with_mrt_and_walls():
@@ -155,4 +190,43 @@ def test_fluctuations_refused_with_mrt_and_walls():
     s.set_fluctuations(None, False, 0, 0, None)
     s.set_collision(_lib.COLL_MRT, mrt_s=np.diag(np.linspace(1.0, 1.4, 9)))
     s.step(2)
+    s.close()
+
+
+def test_zero_generator_state_stays_finite():
+    """A NUMREC stream whose next state is 0 makes the reference's Box-Muller
+    take log(0): the oracle (which restates the reference) gets infinite
+    populations around that cell; the library reads the zero state as state 1
+    for the uniform and stays finite, and every cell the planted cell does not
+    push into equals the oracle.  The stored states are the reference's."""
+    from oracle import oracle as O
+    z, c, nl = load('d2e6_numrec_t12_psi1mexp')
+    seeds = z['seeds_init'].copy()          # cpu ordering: stream + cell * streams
+    ns = seeds.size // int(np.prod(c['dims']))
+    cell = 5 + 24 * 7
+    # the state whose successor is 0: x * 1664525 + 1013904223 = 0 mod 2^32
+    inv = pow(1664525, -1, 2 ** 32)
+    seeds[0 + cell * ns] = np.uint32(((-1013904223) * inv) % 2 ** 32)
+    x, f = XIStencils[c['xi']], FStencils[c['fs']]
+    ora = O.OracleSim(c['dims'], x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], c['G'], tau=c['tau'], psi=c['psi'])
+    ora.set_fields(z['n_init'])
+    ora.init_populations()
+    ora.set_fluctuations(c['kind'], c['indep'], c['kBT'], c['n0'], seeds, c['tau'], nl)
+    with np.errstate(all='ignore'):
+        ora.run(1)
+    want = ora.populations().reshape(9, -1)
+    s = _lib.Sim(2, c['dims'], x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], c['G'],
+                 psi_kind=_lib.PSI_ONE_MINUS_EXP, tau=c['tau'])
+    s.set_density(z['n_init'])
+    s.set_velocity(np.zeros(2 * s.V))
+    s.init_populations()
+    mv, cf = ref_tables(nl, 9, 2)
+    s.set_fluctuations(c['kind'], c['indep'], c['kBT'], c['n0'], seeds, _lib.SEEDS_CELL_MAJOR, mv, cf)
+    s.step(1)
+    got = s.get_populations().reshape(9, -1)
+    assert np.isfinite(got).all()
+    bad = ~np.isfinite(want)
+    assert bad.any()                         # the reference's arithmetic blows up there
+    assert rel_err(got[~bad], want[~bad]) < 1e-12
+    assert np.array_equal(s.get_seeds(_lib.SEEDS_CELL_MAJOR), ora.get_seeds())
     s.close()
