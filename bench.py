@@ -385,6 +385,29 @@ def run_ours(a, dist):
                                 'ms_per_step': round(ms64 / k64, 4),
                                 'kernel_ms': [round(kk[0], 4), round(kk[1], 4)],
                                 'alg_GBs': round(2 * Q * 8 * V * k64 / (ms64 / 1e3) / 1e9, 1)}
+        # the fluctuating step (Gross et al. 2011) on the same box: FP32 single
+        # pass with noise, MINSTD states (one generator per random moment)
+        sf = make_sim('fp32', dev)
+        sf.set_density(n0)
+        sf.set_velocity(np.zeros(3 * V))
+        sf.init_populations()
+        nr, ns = _lib.noise_counts(3, Q, False)
+        seeds = np.random.default_rng(SEED).integers(1, 2 ** 31 - 1, ns * V, dtype=np.uint32)
+        sf.set_fluctuations('MINSTD', False, 1e-5, 1.0, seeds)
+        del seeds
+        sf.step(4)
+        kf = max(20, a.steps // 10)
+        msf = sf.step_timed(kf)
+        kpf = sf.kernels_per_step()
+        sf.close()
+        fb = (2 * Q * 4 + 2 * nr * 4) * V                # populations + generator states, read and written
+        ach_f = fb * kf / (msf / 1e3) / 1e9
+        out['fluctuating'] = {'value': round(V * kf / (msf / 1e3) / 1e6, 1), 'unit': 'MLUPS', 'steps': kf,
+                              'ms_per_step': round(msf / kf, 4), 'kernels_per_step': kpf,
+                              'step': 'Gross 2011 fluctuating BGK (MainLoopGross2011SRT), MINSTD, kBT 1e-5, n0 1',
+                              'kernel': 'k_fused_noise (single pass)' if kpf == 1 else 'k_density_psi + k_fcs_noise',
+                              'alg_bytes_per_cell': (2 * Q * 4 + 2 * nr * 4),
+                              'achieved_GBs': round(ach_f, 1), 'frac': round(ach_f / hbm, 4)}
         out['e2e'] = e2e_measure('fp32', dev)
         if not a.no_cpu:
             out['cpu_baseline'] = cpu_measure(a.cpu_seconds)

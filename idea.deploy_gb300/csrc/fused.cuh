@@ -281,7 +281,8 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
                 if (MRT) collide_cell<L, S, true, float, false>(f, d, n, u, F, q, p, out);
                 else out = bgk_fp32<L, S>(f, u, F, q, p, C0, a, b);
                 if constexpr (NOISE)
-                    add_noise_terms_strided<NR, NT>(z->coef[q], rms, out, std::make_integer_sequence<int, NR>{});
+                    add_noise_terms_strided<NR, NT>(NoiseMask<L>::m(q), z->coef[q], rms, out,
+                                                    std::make_integer_sequence<int, NR>{});
                 // __fsub_rn: no contraction with the product that made `out`
                 // (at omega = 1 it is a plain multiply), so the rest population
                 // balances exactly the rounded values that are stored

@@ -82,6 +82,7 @@ struct KernelOps {
     cudaError_t (*fused_noise)(const void *pop, void *pop_out, const void *step_params, const FusedGeom &fg,
                                void *seeds, const void *noise_params, int grid, cudaStream_t st);
     int (*fused_noise_occupancy)();
+    unsigned (*noise_mask)(int q);  // nonzero pattern the single-pass noise kernel assumes
 };
 
 template <class L, class S, bool MRT, class Real, bool STRICT>
@@ -354,7 +355,7 @@ struct Ops {
                                     f32 ? &batch_add_rest : nullptr, f32 ? &batch_probe : nullptr,
                                     sizeof(NP), MRT ? nullptr : &fill_noise, MRT ? nullptr : &fcs_noise,
                                     &noise_occupancy, (f32 && !MRT) ? &fused_noise : nullptr,
-                                    &fused_noise_occupancy};
+                                    &fused_noise_occupancy, &NoiseMask<L>::m};
         return &o;
     }
 };

@@ -63,6 +63,29 @@ SCLBM_HD constexpr int name_order(int i) {
     return 0;
 }
 
+// Nonzero pattern of the exact noise operator (bit k of m[q]: coef[q][k] != 0),
+// fixed by the lattice; the single-pass kernel skips the other terms.  A table
+// with entries outside it (a reference kernel's literals carry 1e-17 residues)
+// runs the dense two-pass kernel.  tests/test_gross.py checks these against
+// the operator builder.
+template <class L>
+struct NoiseMask;
+template <>
+struct NoiseMask<D2Q9> {
+    SCLBM_HD static constexpr unsigned m(int q) {
+        constexpr unsigned t[9] = {0x25, 0x35, 0x2d, 0x35, 0x2d, 0x3f, 0x3f, 0x3f, 0x3f};
+        return t[q];
+    }
+};
+template <>
+struct NoiseMask<D3Q19> {
+    SCLBM_HD static constexpr unsigned m(int q) {
+        constexpr unsigned t[19] = {0x7029, 0x3329, 0x7869, 0x3329, 0x7869, 0x74a9, 0x74a9, 0x116b, 0x116b, 0x116b,
+                                    0x116b, 0x33ad, 0x33ad, 0x33ad, 0x33ad, 0x7cf9, 0x7cf9, 0x7cf9, 0x7cf9};
+        return t[q];
+    }
+};
+
 template <class L, class Real>
 struct NoiseParams {
     static constexpr int NR = L::Q - L::D - 1;
@@ -194,11 +217,17 @@ __device__ __forceinline__ void add_noise_terms(const Real *coef, const Real *rm
                                                 std::integer_sequence<int, I...>) {
     (add_noise_term<NR, I, Real, STRICT>(coef, rm, acc), ...);
 }
-// FP32 variant reading the moments from a shared-memory slot, rm[k * STRIDE]
+// FP32 variant reading the moments from a shared-memory slot, rm[k * STRIDE],
+// terms outside the lattice's nonzero pattern skipped (q constant after unrolling)
+template <int NR, int STRIDE, int I>
+__device__ __forceinline__ void add_noise_term_masked(unsigned mask, const float *coef, const float *rm, float &acc) {
+    constexpr int k = name_order<NR>(I);
+    if ((mask >> k) & 1u) acc = fmaf(coef[k], rm[k * STRIDE], acc);
+}
 template <int NR, int STRIDE, int... I>
-__device__ __forceinline__ void add_noise_terms_strided(const float *coef, const float *rm, float &acc,
+__device__ __forceinline__ void add_noise_terms_strided(unsigned mask, const float *coef, const float *rm, float &acc,
                                                         std::integer_sequence<int, I...>) {
-    ((acc = fmaf(coef[name_order<NR>(I)], rm[name_order<NR>(I) * STRIDE], acc)), ...);
+    (add_noise_term_masked<NR, STRIDE, I>(mask, coef, rm, acc), ...);
 }
 template <class L, class Real, bool STRICT>
 __device__ __forceinline__ void add_noise(const NoiseParams<L, Real> &z, const Real *rm, Real *out) {

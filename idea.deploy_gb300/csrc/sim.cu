@@ -236,6 +236,7 @@ struct sclbm_sim {
     // fluctuations (sclbm_set_fluctuations): generator kind (0: off), one or two
     // generators per random moment, their states on the device, the noise operator
     int noise_kind = 0, noise_indep = 0, noise_streams = 0;
+    bool noise_sparse = false;      // the operator fits the single-pass kernel's nonzero pattern
     void *seeds = nullptr;
     std::vector<double> noise_m2var, noise_coef;
     std::vector<unsigned char> np;  // noise launch parameter block
@@ -332,7 +333,7 @@ bool fused_fits(const sclbm_sim *s) { return (int64_t)s->Q * s->V < ((int64_t)1 
 
 bool fused_path(const sclbm_sim *s) {
     return s->ops->fused != nullptr && s->path != SCLBM_PATH_TWO_PASS && fused_fits(s) && !s->walls &&
-           (!s->noise_kind || (s->ops->fused_noise != nullptr && !s->noise_indep &&
+           (!s->noise_kind || (s->ops->fused_noise != nullptr && !s->noise_indep && s->noise_sparse &&
                                (int64_t)s->noise_streams * s->V < ((int64_t)1 << 31)));
 }
 
@@ -1203,6 +1204,10 @@ int sclbm_set_fluctuations(sclbm_sim *s, int generator, int indep, double kBT, d
     s->noise_streams = ns;
     s->noise_m2var = mv;
     s->noise_coef = cf;
+    s->noise_sparse = true;
+    for (int q = 0; q < s->Q; q++)
+        for (int k = 0; k < nr; k++)
+            if (cf[(size_t)q * nr + k] != 0.0 && !((s->ops->noise_mask(q) >> k) & 1u)) s->noise_sparse = false;
     s->np.assign(s->ops->noise_size, 0);
     s->ops->fill_noise(s->np.data(), s->noise_kind, s->noise_indep, mv.data(), cf.data());
     s->ngrid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)s->sms * s->ops->noise_occupancy(),

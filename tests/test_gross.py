@@ -157,3 +157,20 @@ def test_generator_streams():
         assert np.array_equal(exp, s1), name
         if c['kind'] == 'MINSTD':
             assert int(z['seeds_200' if 'seeds_200' in z else 'seeds_20'].max()) < 2 ** 31 - 1
+
+
+def test_single_pass_noise_mask_matches_operator():
+    """The compile-time nonzero pattern the single-pass kernel assumes
+    (NoiseMask in noise.cuh) is the exact operator's."""
+    import re
+    src = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                            'idea.deploy_gb300', 'csrc', 'noise.cuh')).read()
+    for lat in ('D2Q9', 'D3Q19'):
+        m = re.search(r'struct NoiseMask<%s> \{.*?constexpr unsigned t\[\d+\] = \{([^}]*)\}' % lat, src, re.S)
+        masks = [int(v, 16) for v in m.group(1).replace('\n', ' ').split(',')]
+        x = XIStencils[lat]
+        D = len(x['XIs'][0])
+        for lit in (_lib.LIT_EXACT, _lib.LIT_ROUND15):
+            _, cf = _lib.noise_operator(D, x['XIs'], x['Ws'], x['c2'], 1.0, 1e-4, 1.0, literals=lit)
+            want = [sum(1 << k for k in range(cf.shape[1]) if cf[q, k] != 0) for q in range(cf.shape[0])]
+            assert masks == want, lat
