@@ -13,6 +13,7 @@
 #include "fused.cuh"
 #include "kernels.cuh"
 #include "noise.cuh"
+#include "simple.cuh"
 
 namespace sclbm {
 
@@ -83,6 +84,18 @@ struct KernelOps {
                                void *seeds, const void *noise_params, int grid, cudaStream_t st);
     int (*fused_noise_occupancy)();
     unsigned (*noise_mask)(int q);  // nonzero pattern the single-pass noise kernel assumes
+    // the "simple" step family (FP64 only, else null)
+    cudaError_t (*simple_inlet)(void *pop, void *dn, void *u, const unsigned char *walls, const SimpleParams &p,
+                                int grid, cudaStream_t st);
+    cudaError_t (*simple_outlet)(void *pop, void *dn, void *u, const unsigned char *walls, const SimpleParams &p,
+                                 int grid, cudaStream_t st);
+    cudaError_t (*simple_moments)(const void *pop, void *dn, void *u, void *psi, const unsigned char *walls,
+                                  const SimpleParams &p, int grid, cudaStream_t st);
+    cudaError_t (*simple_collide)(int sc, int push, const void *pop, void *pop_out, const void *dn, void *u,
+                                  const void *psi, const unsigned char *walls, const SimpleParams &p, int grid,
+                                  cudaStream_t st);
+    cudaError_t (*simple_stream)(const void *pop, void *pop_out, const unsigned char *walls, const SimpleParams &p,
+                                 int grid, cudaStream_t st);
 };
 
 template <class L, class S, bool MRT, class Real, bool STRICT>
@@ -343,6 +356,56 @@ struct Ops {
                                                           0);
         return b > 0 ? b : 1;
     }
+    static constexpr bool F64 = std::is_same<Real, double>::value;
+    static cudaError_t simple_inlet(void *pop, void *dn, void *u, const unsigned char *walls, const SimpleParams &sp,
+                                    int grid, cudaStream_t st) {
+        if constexpr (F64) {
+            k_simple_inlet<L, STRICT><<<grid, 256, 0, st>>>((double *)pop, (double *)dn, (double *)u, walls, sp);
+            return cudaGetLastError();
+        }
+        return cudaErrorNotSupported;
+    }
+    static cudaError_t simple_outlet(void *pop, void *dn, void *u, const unsigned char *walls, const SimpleParams &sp,
+                                     int grid, cudaStream_t st) {
+        if constexpr (F64) {
+            k_simple_outlet<L><<<grid, 256, 0, st>>>((double *)pop, (double *)dn, (double *)u, walls, sp);
+            return cudaGetLastError();
+        }
+        return cudaErrorNotSupported;
+    }
+    static cudaError_t simple_moments(const void *pop, void *dn, void *u, void *psi, const unsigned char *walls,
+                                      const SimpleParams &sp, int grid, cudaStream_t st) {
+        if constexpr (F64) {
+            k_simple_moments<L, STRICT><<<grid, 256, 0, st>>>((const double *)pop, (double *)dn, (double *)u,
+                                                              (double *)psi, walls, sp);
+            return cudaGetLastError();
+        }
+        return cudaErrorNotSupported;
+    }
+    static cudaError_t simple_collide(int sc, int push, const void *pop, void *pop_out, const void *dn, void *u,
+                                      const void *psi, const unsigned char *walls, const SimpleParams &sp, int grid,
+                                      cudaStream_t st) {
+        if constexpr (F64) {
+            const double *a = (const double *)pop, *n = (const double *)dn, *ps = (const double *)psi;
+            double *b = (double *)pop_out, *uu = (double *)u;
+            if (!sc)
+                k_simple_collide<L, S, STRICT, false, true><<<grid, 128, 0, st>>>(a, b, n, uu, ps, walls, sp);
+            else if (push)
+                k_simple_collide<L, S, STRICT, true, true><<<grid, 128, 0, st>>>(a, b, n, uu, ps, walls, sp);
+            else
+                k_simple_collide<L, S, STRICT, true, false><<<grid, 128, 0, st>>>(a, b, n, uu, ps, walls, sp);
+            return cudaGetLastError();
+        }
+        return cudaErrorNotSupported;
+    }
+    static cudaError_t simple_stream(const void *pop, void *pop_out, const unsigned char *walls, const SimpleParams &sp,
+                                     int grid, cudaStream_t st) {
+        if constexpr (F64) {
+            k_simple_stream<L><<<grid, 128, 0, st>>>((const double *)pop, (double *)pop_out, walls, sp);
+            return cudaGetLastError();
+        }
+        return cudaErrorNotSupported;
+    }
     static const KernelOps *ops() {
         constexpr bool f32 = std::is_same<Real, float>::value;
         using SH = FusedShape<L, S>;
@@ -355,7 +418,10 @@ struct Ops {
                                     f32 ? &batch_add_rest : nullptr, f32 ? &batch_probe : nullptr,
                                     sizeof(NP), MRT ? nullptr : &fill_noise, MRT ? nullptr : &fcs_noise,
                                     &noise_occupancy, (f32 && !MRT) ? &fused_noise : nullptr,
-                                    &fused_noise_occupancy, &NoiseMask<L>::m};
+                                    &fused_noise_occupancy, &NoiseMask<L>::m,
+                                    F64 ? &simple_inlet : nullptr, F64 ? &simple_outlet : nullptr,
+                                    F64 ? &simple_moments : nullptr, F64 ? &simple_collide : nullptr,
+                                    F64 ? &simple_stream : nullptr};
         return &o;
     }
 };

@@ -242,6 +242,9 @@ struct sclbm_sim {
     std::vector<unsigned char> np;  // noise launch parameter block
     int ngrid = 0;                  // noise kernel grid (resident CTAs, capped by the cells)
     double tau_bgk = 1.0;           // BGK relaxation time of the current operator
+    // the "simple" step family (sclbm_set_simple): 0 off, SCLBM_SIMPLE_GUO / _SC
+    int simple_mode = 0, simple_inout = 0, simple_walls = 0;
+    SimpleParams spar = {};
     double *red = nullptr;
     int red_blocks = 0;
     int dgrid = 0, fgrid = 0, ugrid = 0;
@@ -333,6 +336,7 @@ bool fused_fits(const sclbm_sim *s) { return (int64_t)s->Q * s->V < ((int64_t)1 
 
 bool fused_path(const sclbm_sim *s) {
     return s->ops->fused != nullptr && s->path != SCLBM_PATH_TWO_PASS && fused_fits(s) && !s->walls &&
+           !s->simple_mode &&
            (!s->noise_kind || (s->ops->fused_noise != nullptr && !s->noise_indep && s->noise_sparse &&
                                (int64_t)s->noise_streams * s->V < ((int64_t)1 << 31)));
 }
@@ -344,10 +348,60 @@ cudaError_t density_pass(sclbm_sim *s) {
     return s->ops->density(s->pop[s->cur], s->dn, s->psi, s->sp.data(), s->dgrid, s->st);
 }
 
+// the SC inlet/outlet loop streams before it collides (MultiPhase.py:735-887)
+bool simple_stream_first(const sclbm_sim *s) { return s->simple_mode == SCLBM_SIMPLE_SC && s->simple_inout; }
+
+int simple_kernels(const sclbm_sim *s) {
+    if (simple_stream_first(s)) return 5;
+    return (s->simple_inout ? 2 : 0) + 2;
+}
+
+// one step of the simple family; ev (optional) gets an event after each kernel
+int launch_simple(sclbm_sim *s, cudaEvent_t *ev) {
+    const KernelOps *o = s->ops;
+    const SimpleParams &p = s->spar;
+    const int sc = s->simple_mode == SCLBM_SIMPLE_SC;
+    const unsigned char *walls = s->simple_walls ? s->walls : nullptr;
+    void *cur = s->pop[s->cur], *nxt = s->pop[s->cur ^ 1];
+    int k = 0;
+    cudaError_t e = cudaSuccess;
+    auto mark = [&]() {
+        if (ev && e == cudaSuccess) e = cudaEventRecord(ev[k], s->st);
+        k++;
+    };
+    if (simple_stream_first(s)) {
+        e = o->simple_outlet(cur, s->dn, s->u, walls, p, s->dgrid, s->st);
+        mark();
+        if (e == cudaSuccess) e = o->simple_inlet(cur, s->dn, s->u, walls, p, s->dgrid, s->st);
+        mark();
+        if (e == cudaSuccess) e = o->simple_stream(cur, nxt, walls, p, s->fgrid, s->st);
+        mark();
+        if (e == cudaSuccess) e = o->simple_moments(nxt, s->dn, s->u, s->psi, walls, p, s->dgrid, s->st);
+        mark();
+        if (e == cudaSuccess) e = o->simple_collide(sc, 0, nxt, nxt, s->dn, s->u, s->psi, walls, p, s->fgrid, s->st);
+        mark();
+    } else {
+        if (s->simple_inout) {
+            e = o->simple_inlet(cur, s->dn, s->u, walls, p, s->dgrid, s->st);
+            mark();
+            if (e == cudaSuccess) e = o->simple_outlet(cur, s->dn, s->u, walls, p, s->dgrid, s->st);
+            mark();
+        }
+        if (e == cudaSuccess) e = o->simple_moments(cur, s->dn, s->u, s->psi, walls, p, s->dgrid, s->st);
+        mark();
+        if (e == cudaSuccess) e = o->simple_collide(sc, 1, cur, nxt, s->dn, s->u, s->psi, walls, p, s->fgrid, s->st);
+        mark();
+    }
+    if (e != cudaSuccess) return fail(SCLBM_ERR_CUDA, "step launch: %s", cudaGetErrorString(e));
+    s->cur ^= 1;
+    return SCLBM_OK;
+}
+
 // enqueue the kernels of one step; ev (optional) gets an event after each kernel
 int launch_step(sclbm_sim *s, cudaEvent_t *ev = nullptr) {
     const KernelOps *o = s->ops;
     cudaError_t e;
+    if (s->simple_mode) return launch_simple(s, ev);
     if (fused_path(s)) {
         if (s->noise_kind)
             e = o->fused_noise(s->pop[s->cur], s->pop[s->cur ^ 1], s->sp.data(), s->fg, s->seeds, s->np.data(),
@@ -605,6 +659,8 @@ int configure(sclbm_sim *s, int collision, double tau, const double *mrt_s, cons
     if (!ops) return fail(SCLBM_ERR_UNSUPPORTED, "no kernels for this configuration");
     if (s->noise_kind && !ops->fcs_noise)
         return fail(SCLBM_ERR_UNSUPPORTED, "the fluctuating step is BGK only (switch the fluctuations off first)");
+    if (s->simple_mode && mrt)
+        return fail(SCLBM_ERR_UNSUPPORTED, "the simple step family is BGK (switch it off first)");
     bool a_nonzero = false;
     for (int q = 0; q < s->Q; q++) a_nonzero = a_nonzero || t.A[(size_t)q * s->Q + q] != 0.0;
     HostSetup h;
@@ -799,7 +855,7 @@ int sclbm_info(const sclbm_sim *s, int64_t *volume, int64_t *device_bytes) {
 
 int sclbm_kernels_per_step(const sclbm_sim *s, int *count) {
     if (!s || !count) return fail(SCLBM_ERR_ARG, "null argument");
-    *count = fused_path(s) ? 1 : 2;
+    *count = s->simple_mode ? simple_kernels(s) : fused_path(s) ? 1 : 2;
     return SCLBM_OK;
 }
 
@@ -889,8 +945,13 @@ int sclbm_step(sclbm_sim *s, int64_t nsteps) {
     if (nsteps < 0) return fail(SCLBM_ERR_ARG, "nsteps < 0");
     if (!s->pop_set) return fail(SCLBM_ERR_STATE, "populations are not initialized");
     DevGuard dg(s->device);
-    s->moments_fresh = s->dn_fresh = false;
-    return run_steps(s, nsteps);
+    // the simple family leaves in n and u what the reference's loops leave there
+    // (the moments at the start of the last step, the stored velocity)
+    const bool keep = s->simple_mode && nsteps > 0;
+    if (!keep) s->moments_fresh = s->dn_fresh = false;
+    const int rc = run_steps(s, nsteps);
+    if (keep && !rc) s->moments_fresh = s->dn_fresh = true;
+    return rc;
 }
 
 int sclbm_sync(sclbm_sim *s) {
@@ -915,7 +976,7 @@ int sclbm_step_timed(sclbm_sim *s, int64_t nsteps, double *ms) {
     cudaEventElapsedTime(&t, e0, e1);
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
-    s->moments_fresh = s->dn_fresh = false;
+    s->moments_fresh = s->dn_fresh = s->simple_mode && nsteps > 0 && rc == SCLBM_OK;
     *ms = t;
     if (rc) return rc;
     CUDA_TRY(cudaGetLastError());
@@ -926,6 +987,7 @@ int sclbm_profile_step(sclbm_sim *s, int64_t nsteps, double *ms, int nms) {
     if (!s || !ms || nms < 2) return fail(SCLBM_ERR_ARG, "bad argument");
     if (!s->pop_set) return fail(SCLBM_ERR_STATE, "populations are not initialized");
     if (nsteps < 1 || nsteps > 4096) return fail(SCLBM_ERR_ARG, "nsteps in [1, 4096]");
+    if (s->simple_mode) return fail(SCLBM_ERR_UNSUPPORTED, "per-kernel times of the simple step family");
     DevGuard dg(s->device);
     // per step: an event before the step, then one after each kernel
     std::vector<cudaEvent_t> ev((size_t)nsteps * 3);
@@ -1085,8 +1147,9 @@ int sclbm_set_walls(sclbm_sim *s, const int *walls, const double *psi) {
     if (!s || !walls || !psi) return fail(SCLBM_ERR_ARG, "null argument");
     if (s->noise_kind) return fail(SCLBM_ERR_UNSUPPORTED, "walls with fluctuations (the reference has no such step)");
     for (int64_t g = 0; g < s->V; g++)
-        if (walls[g] != 0 && walls[g] != 1) return fail(SCLBM_ERR_ARG, "walls[%lld] = %d (1 fluid, 0 wall)",
-                                                        (long long)g, walls[g]);
+        if (walls[g] < 0 || walls[g] > 3)
+            return fail(SCLBM_ERR_ARG, "walls[%lld] = %d (1 fluid, 0 wall, 2 inlet, 3 outlet)", (long long)g,
+                        walls[g]);
     DevGuard dg(s->device);
     int rc = SCLBM_OK;
     if (!s->walls) rc = alloc(s, (void **)&s->walls, (size_t)s->V);
@@ -1158,6 +1221,7 @@ int sclbm_set_fluctuations(sclbm_sim *s, int generator, int indep, double kBT, d
     if ((m2var == nullptr) != (coef == nullptr)) return fail(SCLBM_ERR_ARG, "m2var and coef go together");
     if (s->mrt || !s->ops->fcs_noise) return fail(SCLBM_ERR_UNSUPPORTED, "the fluctuating step is BGK only");
     if (s->walls) return fail(SCLBM_ERR_UNSUPPORTED, "walls with fluctuations (the reference has no such step)");
+    if (s->simple_mode) return fail(SCLBM_ERR_UNSUPPORTED, "fluctuations with the simple step family");
     if (!(kBT >= 0) || !std::isfinite(kBT) || !std::isfinite(n0)) return fail(SCLBM_ERR_ARG, "kBT %g, n0 %g", kBT, n0);
     const int nr = s->Q - s->D - 1, ns = indep ? 2 * nr : nr;
     std::vector<double> mv, cf;
@@ -1232,6 +1296,53 @@ int sclbm_get_seeds(sclbm_sim *s, void *seeds, int layout) {
             const size_t dst = layout == SCLBM_SEEDS_STREAM_MAJOR ? k * s->V + g : g * ns + k;
             std::memcpy((unsigned char *)seeds + dst * es, host.data() + src * es, es);
         }
+    return SCLBM_OK;
+}
+
+int sclbm_set_simple(sclbm_sim *s, int forcing, int use_walls, int gravity, double g, int inlet_outlet,
+                     double u_in) {
+    if (!s) return fail(SCLBM_ERR_ARG, "null handle");
+    DevGuard dg(s->device);
+    CUDA_TRY(cudaStreamSynchronize(s->st));
+    for (auto &gr : s->graph)
+        if (gr) cudaGraphExecDestroy(gr), gr = nullptr;  // the step's kernels change
+    if (forcing == SCLBM_SIMPLE_OFF) {
+        s->simple_mode = s->simple_inout = 0;
+        return SCLBM_OK;
+    }
+    if (forcing != SCLBM_SIMPLE_GUO && forcing != SCLBM_SIMPLE_SC) return fail(SCLBM_ERR_ARG, "forcing %d", forcing);
+    if (s->fp32 || !s->ops->simple_collide) return fail(SCLBM_ERR_UNSUPPORTED, "the simple step family is FP64");
+    if (s->mrt) return fail(SCLBM_ERR_UNSUPPORTED, "the simple step family is BGK");
+    if (s->noise_kind) return fail(SCLBM_ERR_UNSUPPORTED, "the simple step family with fluctuations");
+    if (gravity && forcing != SCLBM_SIMPLE_GUO)
+        return fail(SCLBM_ERR_UNSUPPORTED, "gravity goes with Guo forcing (MainLoopSimpleWallsGravity)");
+    if (gravity && inlet_outlet) return fail(SCLBM_ERR_UNSUPPORTED, "gravity with inlet/outlet");
+    if ((inlet_outlet || use_walls) && !s->walls) return fail(SCLBM_ERR_STATE, "no walls set (sclbm_set_walls)");
+    if (inlet_outlet && !use_walls) return fail(SCLBM_ERR_ARG, "inlet/outlet flags are wall flags");
+    if (!std::isfinite(g) || !std::isfinite(u_in)) return fail(SCLBM_ERR_ARG, "g %g, u_in %g", g, u_in);
+    if (inlet_outlet) {
+        // every outlet cell copies the cell at x - 1
+        std::vector<unsigned char> w(s->V);
+        CUDA_TRY(cudaMemcpyAsync(w.data(), s->walls, s->V, cudaMemcpyDeviceToHost, s->st));
+        CUDA_TRY(cudaStreamSynchronize(s->st));
+        for (int64_t c = 0; c < s->V; c++)
+            if (w[c] == 3 && c % s->L[0] == 0) return fail(SCLBM_ERR_ARG, "outlet cell %lld at x = 0", (long long)c);
+    }
+    SimpleParams &p = s->spar;
+    p = SimpleParams{};
+    for (int d = 0; d < 3; d++) p.geo.L[d] = d < s->D ? s->L[d] : 1;
+    p.geo.V = s->V;
+    for (int q = 0; q < s->Q; q++) p.w[q] = s->w[q];
+    for (int a = 0; a < s->QE; a++) p.we[a] = s->we[a];
+    p.neg_g = -s->G;
+    p.omega = 1.0 / s->tau_bgk;
+    p.g = g;
+    p.u_in = u_in;
+    p.psi_kind = s->psi_kind;
+    p.gravity = gravity ? 1 : 0;
+    s->simple_mode = forcing;
+    s->simple_inout = inlet_outlet ? 1 : 0;
+    s->simple_walls = use_walls ? 1 : 0;
     return SCLBM_OK;
 }
 

@@ -46,6 +46,14 @@ _PSI_CODES = {
     '1-exp(-ln_0)': _lib.PSI_ONE_MINUS_EXP,
     '1.0-exp(-ln_0)': _lib.PSI_ONE_MINUS_EXP,
     'ln_0': _lib.PSI_IDENTITY,
+    # the simple step family's kernels name the density ln
+    'exp(-1./ln)': _lib.PSI_EXP_INV,
+    'exp(-1/ln)': _lib.PSI_EXP_INV,
+    'exp(-1.0/ln)': _lib.PSI_EXP_INV,
+    '1.-exp(-ln)': _lib.PSI_ONE_MINUS_EXP,
+    '1-exp(-ln)': _lib.PSI_ONE_MINUS_EXP,
+    '1.0-exp(-ln)': _lib.PSI_ONE_MINUS_EXP,
+    'ln': _lib.PSI_IDENTITY,
 }
 
 
@@ -250,6 +258,7 @@ class ShanChenMultiPhase:
         if self.crng is None:
             raise Exception("Fluctuations not set up: construct with fluctuations='Gross2011'")
         self._check_init()
+        self._simple_off()
         if self._collision != ('bgk', self.params_dict['tau']):
             self._sim.set_collision(_lib.COLL_BGK, tau=self.params_dict['tau'])
             self._collision = ('bgk', self.params_dict['tau'])
@@ -355,6 +364,7 @@ class ShanChenMultiPhase:
     def MainLoop(self, time_steps, convergence_functions=[], profiling=False):
         self._check_init()
         self._noise_off()
+        self._simple_off()
         if self._collision != ('bgk', self.params_dict['tau']) and self._collision != ('tables',):
             self._sim.set_collision(_lib.COLL_BGK, tau=self.params_dict['tau'])
             self._collision = ('bgk', self.params_dict['tau'])
@@ -368,6 +378,7 @@ class ShanChenMultiPhase:
             raise Exception("Missing argument 'omega_syms_vals'")
         self._check_init()
         self._noise_off()
+        self._simple_off()
         S = numeric_relaxation_matrix(relaxation_matrix, omega_syms_vals, self.sims_vars['Q'])
         key = ('mrt', S.tobytes())
         if self._collision != key:
@@ -392,6 +403,76 @@ class ShanChenMultiPhase:
         if not getattr(self, '_walls', False):
             raise Exception("Walls not set (GetWalls)")
         return self.MainLoop(time_steps, convergence_functions, profiling)
+
+    # ---- the simple step family (MainLoopSimple*, idpy/LBM/MultiPhase.py:164-1014) ----
+    def _simple_off(self):
+        if getattr(self, '_simple', None) is not None:
+            self._sim.set_simple(_lib.SIMPLE_OFF)
+            self._simple = None
+
+    def _simple_loop(self, key, time_steps, convergence_functions, profiling, convergence_functions_args=()):
+        forcing, use_walls, gravity, inout, u_in = key
+        if use_walls and not getattr(self, '_walls', False):
+            raise Exception("Walls not set (GetWalls)")
+        self._check_init()
+        self._noise_off()
+        if self._collision != ('bgk', self.params_dict['tau']):
+            self._sim.set_collision(_lib.COLL_BGK, tau=self.params_dict['tau'])
+            self._collision = ('bgk', self.params_dict['tau'])
+        if getattr(self, '_simple', None) != key:
+            self._sim.set_simple(forcing, use_walls=use_walls, gravity=gravity, inlet_outlet=inout, u_in=u_in)
+            self._simple = key
+        if convergence_functions_args:
+            fns = [lambda lbm, f=f, kw=kw: f(lbm, **kw) for f, kw in zip(convergence_functions,
+                                                                          convergence_functions_args)]
+        else:
+            fns = convergence_functions
+        return self._loop(time_steps, fns, profiling)
+
+    def MainLoopSimple(self, time_steps, convergence_functions=[], profiling=False):
+        """Moments, psi, in-place BGK collision with Guo forcing, periodic
+        stream (idpy/LBM/MultiPhase.py:164-255)."""
+        return self._simple_loop((_lib.SIMPLE_GUO, False, None, False, 0.0), time_steps, convergence_functions,
+                                 profiling)
+
+    def MainLoopSimpleSC(self, time_steps, convergence_functions=[], profiling=False):
+        """As MainLoopSimple with the Shan-Chen velocity shift
+        (u_eq = u + F/(n omega); idpy/LBM/MultiPhase.py:257-349)."""
+        return self._simple_loop((_lib.SIMPLE_SC, False, None, False, 0.0), time_steps, convergence_functions,
+                                 profiling)
+
+    def MainLoopSimpleWalls(self, time_steps, convergence_functions=[], profiling=False):
+        """MainLoopSimple on the fluid cells of GetWalls with halfway
+        bounce-back (idpy/LBM/MultiPhase.py:351-465)."""
+        return self._simple_loop((_lib.SIMPLE_GUO, True, None, False, 0.0), time_steps, convergence_functions,
+                                 profiling)
+
+    def MainLoopSimpleWallsSC(self, time_steps, convergence_functions=[], profiling=False):
+        """(idpy/LBM/MultiPhase.py:467-581)"""
+        return self._simple_loop((_lib.SIMPLE_SC, True, None, False, 0.0), time_steps, convergence_functions,
+                                 profiling)
+
+    def MainLoopSimpleWallsGravity(self, time_steps, convergence_functions=[], g=0, profiling=False):
+        """MainLoopSimpleWalls with gravity g added to F_y of every non-wall
+        cell (idpy/LBM/MultiPhase.py:888-1013)."""
+        return self._simple_loop((_lib.SIMPLE_GUO, True, float(g), False, 0.0), time_steps,
+                                 convergence_functions, profiling)
+
+    def MainLoopSimpleWallsInletOutlet(self, time_steps, convergence_functions=[], profiling=False, n_in=1, u_in=0,
+                                       tau_in=100, max_mult=2):
+        """Walls with an inlet (flag 2: n = 2, u = (u_in, 0, ..), equilibrium)
+        and an outlet (flag 3: the cell at x - 1) (idpy/LBM/MultiPhase.py:583-733).
+        n_in, tau_in and max_mult are accepted and unused, as in the
+        reference's inlet kernel (LBMKernels.py:299-357)."""
+        return self._simple_loop((_lib.SIMPLE_GUO, True, None, True, float(u_in)), time_steps,
+                                 convergence_functions, profiling)
+
+    def MainLoopSimpleWallsInletOutletSC(self, time_steps, convergence_functions=[], convergence_functions_args=[],
+                                         profiling=False, n_in=1, u_in=0, tau_in=100, max_mult=2):
+        """The Shan-Chen-forcing inlet/outlet loop; it streams before it
+        collides (idpy/LBM/MultiPhase.py:735-887)."""
+        return self._simple_loop((_lib.SIMPLE_SC, True, None, True, float(u_in)), time_steps,
+                                 convergence_functions, profiling, convergence_functions_args)
 
     # ---- read-back / observables --------------------------------------------
     def ComputeMomentsMeta(self):

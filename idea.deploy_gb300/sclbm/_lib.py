@@ -20,6 +20,7 @@ LIT_ROUND15, LIT_EXACT = 0, 1
 CRNG_NONE, CRNG_MINSTD, CRNG_NUMREC, CRNG_MMIX = 0, 1, 2, 3
 CRNG_KINDS = {'MINSTD': CRNG_MINSTD, 'NUMREC': CRNG_NUMREC, 'MMIX': CRNG_MMIX}
 SEEDS_STREAM_MAJOR, SEEDS_CELL_MAJOR = 0, 1
+SIMPLE_OFF, SIMPLE_GUO, SIMPLE_SC = 0, 1, 2
 
 
 class SclbmError(RuntimeError):
@@ -104,6 +105,7 @@ SIGNATURES = {
     'sclbm_noise_operator': [ctypes.POINTER(Params), _D, _D, _P, _P],
     'sclbm_set_fluctuations': [_P, ctypes.c_int, ctypes.c_int, _D, _D, _P, ctypes.c_int, _P, _P],
     'sclbm_get_seeds': [_P, _P, ctypes.c_int],
+    'sclbm_set_simple': [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _D, ctypes.c_int, _D],
     'sclbm_mlp_param_count': [_IP],
     'sclbm_mlp_create': [ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(_P)],
     'sclbm_mlp_destroy': [_P],
@@ -357,6 +359,13 @@ class Sim:
         out = np.empty(ns * self.V, dt)
         call('sclbm_get_seeds', self.h, ptr(out), int(layout))
         return out
+
+    def set_simple(self, forcing, use_walls=False, gravity=None, inlet_outlet=False, u_in=0.0):
+        """The reference's simple step family: forcing SIMPLE_GUO / SIMPLE_SC
+        (SIMPLE_OFF: back to the generated-kernel step), gravity along y (Guo),
+        inlet / outlet wall flags 2 / 3 with inlet velocity u_in."""
+        call('sclbm_set_simple', self.h, int(forcing), int(bool(use_walls)), int(gravity is not None),
+             float(gravity or 0.0), int(bool(inlet_outlet)), float(u_in))
 
     def restore_mass(self, target=float('nan')):
         """FP64 mass before; if target is finite, restore it (rest populations)."""

@@ -39,6 +39,7 @@
  *                           MainLoopGross2011SRT idpy/LBM/MultiPhase.py:1404-1541,2029-2069,
  *                                           idpy/PRNGS/CRNGS.py:87-337
  *   sclbm_get_seeds         crng.sims_idpy_memory['seeds'].D2H()
+ *   sclbm_set_simple        MainLoopSimple* loops  idpy/LBM/MultiPhase.py:164-1014
  *   sclbm_destroy           End()            idpy/LBM/MultiPhase.py:2171-2175
  */
 #ifndef SCLBM_H
@@ -154,12 +155,35 @@ SCLBM_API int sclbm_init_cylinder(sclbm_sim *s, double n_g, double n_l, double R
                         int full_flag);
 
 /* walls (GetWalls, idpy/LBM/MultiPhase.py:157-162, and then every step as
- * MainLoopWalls, :1226-1309): walls[V] = 1 fluid, 0 wall; psi[V] the psi
+ * MainLoopWalls, :1226-1309): walls[V] = 1 fluid, 0 wall (2 inlet, 3 outlet for
+ * the simple step family, which treats them as neither); psi[V] the psi
  * field, which wall cells keep (their wetting).  From then on density and psi
  * are computed on fluid cells only, the step runs on fluid cells only and a
  * population pushed into a wall returns to the opposite population of its own
  * cell (halfway bounce-back); the two-pass kernels run (no single pass). */
 SCLBM_API int sclbm_set_walls(sclbm_sim *s, const int *walls, const double *psi);
+
+/* the reference's "simple" step family (MainLoopSimple, MainLoopSimpleSC,
+ * MainLoopSimpleWalls[SC], MainLoopSimpleWallsGravity,
+ * MainLoopSimpleWallsInletOutlet[SC]; idpy/LBM/MultiPhase.py:164-1014, kernels
+ * idpy/LBM/MultiPhaseKernels.py:132-604, idpy/LBM/LBMKernels.py:117-258,299-456):
+ * moments on fluid cells, psi on non-wall cells, an in-place BGK collision with
+ * Guo forcing (SCLBM_SIMPLE_GUO) or the Shan-Chen velocity shift
+ * (SCLBM_SIMPLE_SC), the periodic stream and halfway bounce-back.  gravity != 0
+ * adds g to F_y and collides every non-wall cell (Guo only).  inlet_outlet != 0:
+ * wall flags 2 (inlet: n = 2, u = (u_in, 0, ..), equilibrium) and 3 (outlet: the
+ * cell at x - 1) are set each step; with SCLBM_SIMPLE_SC the step then streams
+ * before it collides, as the reference's loop does.  FP64 only (its arithmetic,
+ * in the reference's order with SCLBM_LIT_ROUND15).  After steps of this family
+ * the density and velocity read back are the arrays the reference's loops leave
+ * (the moments at the start of the last step, the stored velocity).
+ * use_walls = 0: every cell fluid (MainLoopSimple[SC], which ignore walls).
+ * SCLBM_SIMPLE_OFF returns to the generated-kernel step. */
+#define SCLBM_SIMPLE_OFF 0
+#define SCLBM_SIMPLE_GUO 1
+#define SCLBM_SIMPLE_SC  2
+SCLBM_API int sclbm_set_simple(sclbm_sim *s, int forcing, int use_walls, int gravity, double g, int inlet_outlet,
+                               double u_in);
 
 /* fluctuations: the Gross et al. (2011) fluctuating step
  * (MainLoopGross2011SRT, idpy/LBM/MultiPhase.py:1404-1541; its kernel

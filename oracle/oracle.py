@@ -25,6 +25,9 @@ What is restated where:
   * initial profiles: idpy/LBM/MultiPhaseKernels.py:44-112,605-777
   * CheckUConvergenceSCMP: idpy/LBM/MultiPhaseLoopChecks.py:96-163
   * DeltaPLaplace / PBulk / ComputeCenterOfMass: idpy/LBM/MultiPhase.py:108-137,1690-1768
+  * the "simple" step family (MainLoopSimple*, idpy/LBM/MultiPhase.py:164-1014):
+    ``OracleSimple``  idpy/LBM/MultiPhaseKernels.py:132-604,
+    idpy/LBM/LBMKernels.py:117-258,299-456
   * Gross et al. (2011) fluctuations: ``noise_terms``, ``noise_variance``,
     ``OracleSim.set_fluctuations``  idpy/LBM/Fluctuations.py:40-165,
     idpy/PRNGS/CRNGS.py:603-1276, idpy/LBM/MultiPhaseKernelsMeta.py:1369-1557
@@ -666,3 +669,64 @@ def init_cylinder(dims, n_g, n_l, R, direction=0, full_flag=True):
     r = np.sqrt(r2.astype(np.float64))
     dn = (n_l - n_g) if full_flag else (n_g - n_l)
     return 0.5 * (n_g + n_l) - 0.5 * dn * np.tanh(r - R)
+
+
+class _Simple(ctypes.Structure):
+    _fields_ = [('dim', ctypes.c_int), ('L', ctypes.c_int * 3), ('Q', ctypes.c_int), ('QE', ctypes.c_int),
+                ('xi', ctypes.c_void_p), ('w', ctypes.c_void_p), ('e', ctypes.c_void_p), ('we', ctypes.c_void_p),
+                ('opposite', ctypes.c_void_p), ('G', ctypes.c_double), ('omega', ctypes.c_double),
+                ('psi_kind', ctypes.c_int), ('forcing', ctypes.c_int), ('gravity', ctypes.c_int),
+                ('g', ctypes.c_double), ('inout', ctypes.c_int), ('u_in', ctypes.c_double), ('order', ctypes.c_int)]
+
+
+class OracleSimple:
+    """The reference's "simple" step family on the CPU (q-major arrays, as its
+    kernels index them): MainLoopSimple[SC] (no walls), MainLoopSimpleWalls[SC],
+    MainLoopSimpleWallsGravity, MainLoopSimpleWallsInletOutlet[SC]
+    (idpy/LBM/MultiPhase.py:164-1014).  forcing 'guo' or 'sc'; walls flags
+    1 fluid, 0 wall, 2 inlet, 3 outlet (shape flip(dims)) or None."""
+
+    def __init__(self, dims, xi, w, e, we, G, tau=1.0, psi='exp', walls=None, psi_w=None, forcing='guo',
+                 gravity=None, u_in=None):
+        self.dims = tuple(int(x) for x in dims)
+        self.D, self.Q = len(self.dims), len(xi)
+        self.V = int(np.prod(self.dims))
+        xi = [tuple(int(v) for v in x) for x in xi]
+        self._xi = np.array(xi, np.int32).ravel()
+        self._w = np.array(w, np.float64)
+        self._e = np.array(e, np.int32).ravel()
+        self._we = np.array(we, np.float64)
+        self._opp = np.array([xi.index(tuple(-v for v in x)) for x in xi], np.int32)
+        self.walls = np.ones(self.V, np.int32) if walls is None else \
+            np.ascontiguousarray(np.asarray(walls, np.int32).ravel())
+        self.pop = np.zeros(self.Q * self.V)
+        self.pop_b = np.zeros(self.Q * self.V)
+        self.n = np.zeros(self.V)
+        self.u = np.zeros(self.D * self.V)
+        self.psi = np.zeros(self.V) if psi_w is None else np.array(psi_w, np.float64).ravel().copy()
+        c = _Simple()
+        c.dim = self.D
+        for d in range(3):
+            c.L[d] = self.dims[d] if d < self.D else 1
+        c.Q, c.QE = self.Q, len(self._we)
+        c.xi, c.w, c.e, c.we, c.opposite = _ptr(self._xi), _ptr(self._w), _ptr(self._e), _ptr(self._we), \
+            _ptr(self._opp)
+        c.G, c.omega, c.psi_kind = float(G), 1.0 / tau, PSI_KINDS[psi]
+        c.forcing = {'guo': 0, 'sc': 1}[forcing]
+        c.gravity, c.g = (0, 0.0) if gravity is None else (1, float(gravity))
+        c.inout, c.u_in = (0, 0.0) if u_in is None else (1, float(u_in))
+        # MainLoopSimpleWallsInletOutletSC: outlet, inlet, stream, bounce, moments, psi, collide
+        c.order = 1 if (u_in is not None and forcing == 'sc') else 0
+        self.cfg = c
+
+    def set_state(self, pop, n, u=None):
+        self.pop[:] = np.asarray(pop, np.float64).ravel()
+        self.n[:] = np.asarray(n, np.float64).ravel()
+        self.u[:] = 0.0 if u is None else np.asarray(u, np.float64).ravel()
+
+    def run(self, nsteps):
+        sw = ctypes.c_int(0)
+        lib().orc_simple_run(ctypes.byref(self.cfg), _ptr(self.pop), _ptr(self.pop_b), _ptr(self.n), _ptr(self.u),
+                             _ptr(self.psi), _ptr(self.walls), int(nsteps), ctypes.byref(sw))
+        if sw.value:
+            self.pop, self.pop_b = self.pop_b, self.pop

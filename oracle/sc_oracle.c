@@ -407,3 +407,219 @@ int orc_run_noise(const orc_cfg *c, const orc_noise *z, double *pop_a, double *p
     *swapped = (cur != pop_a);
     return 0;
 }
+
+/* ---- the "simple" step family (MainLoopSimple*, idpy/LBM/MultiPhase.py:164-1014) ----
+ * Hand-written kernels over q-major arrays (pop[g + q*V], u[g + d*V]), run in this order
+ * each step (IdpyLoop.Run, serial on the CTypes backend):
+ *   inlet   K_SetPopNUXInletDutyCycle   LBMKernels.py:299-357   (walls == 2: n = 2, u = (u_in, 0..), equilibrium)
+ *   outlet  K_SetPopNUOutletNoGradient  LBMKernels.py:423-456   (walls == 3: n, u, pop of the cell at x - 1)
+ *   moments K_ComputeMoments[Walls]     LBMKernels.py:187-258   (walls == 1)
+ *   psi     K_ComputePsi[Walls]         MultiPhaseKernels.py:562-604 (walls != 0)
+ *   collide K_Collision_ShanChen[Guo]MultiPhase[Walls][Gravity]  MultiPhaseKernels.py:132-561
+ *           in place, Guo forcing or the Shan-Chen velocity shift; gravity adds g to F_y
+ *           (and that kernel collides every cell with walls != 0)
+ *   stream  K_StreamPeriodic (pull)     LBMKernels.py:117-149
+ *   bounce  K_HalfWayBounceBack         LBMKernels.py:151-185  (walls == 0)
+ * MainLoopSimpleWallsInletOutletSC (MultiPhase.py:735-887) runs them in another order:
+ * outlet, inlet, stream, bounce, swap, moments, psi, collide (the step ends after the
+ * collision) -- order 1 below.
+ * Every expression keeps the reference's operand order; CM2 = 3.0, CM4 = 9.0. */
+typedef struct {
+    int dim, L[3], Q, QE;
+    const int *xi;        /* Q*dim */
+    const double *w;      /* Q */
+    const int *e;         /* QE*dim */
+    const double *we;     /* QE */
+    const int *opposite;  /* Q */
+    double G, omega;
+    int psi_kind;
+    int forcing;          /* 0 Guo, 1 Shan-Chen velocity shift */
+    int gravity;          /* 1: F_y += g and collide walls != 0 */
+    double g;
+    int inout;            /* 1: inlet (walls 2) and outlet (walls 3) setters */
+    double u_in;
+    int order;            /* 0: set, moments, psi, collide, stream, bounce; 1: the SC inlet/outlet order */
+} orc_simple;
+
+static inline void s_pos(const orc_simple *c, long g, int *p) {
+    p[0] = (int)(g % c->L[0]);
+    if (c->dim > 1) p[1] = (int)((g / c->L[0]) % c->L[1]);
+    if (c->dim > 2) p[2] = (int)(g / ((long)c->L[0] * c->L[1]));
+}
+static inline long s_index(const orc_simple *c, const int *p) {
+    long i = p[0];
+    if (c->dim > 1) i += (long)p[1] * c->L[0];
+    if (c->dim > 2) i += (long)p[2] * c->L[0] * c->L[1];
+    return i;
+}
+
+static void s_inlet(const orc_simple *c, long V, double *pop, double *n, double *u, const int *walls) {
+    const int D = c->dim, Q = c->Q;
+    for (long g = 0; g < V; g++) {
+        if (walls[g] != 2) continue;
+        const double ln = n[g] = 2.;
+        const double u_swap = c->u_in;
+        double lu[3];
+        const double u_dot_u = u_swap * u_swap;
+        lu[0] = u[g] = u_swap;
+        for (int d = 1; d < D; d++) lu[d] = u[g + d * V] = 0.;
+        for (int q = 0; q < Q; q++) {
+            double u_dot_xi = 0.;
+            for (int d = 0; d < D; d++) u_dot_xi += lu[d] * c->xi[d + q * D];
+            double leq = 1.;
+            leq += u_dot_xi * 3.0;
+            leq += 0.5 * u_dot_xi * u_dot_xi * 9.0;
+            leq -= 0.5 * u_dot_u * 3.0;
+            leq = leq * ln * c->w[q];
+            pop[g + q * V] = leq;
+        }
+    }
+}
+
+static void s_outlet(const orc_simple *c, long V, double *pop, double *n, double *u, const int *walls) {
+    const int D = c->dim, Q = c->Q;
+    for (long g = 0; g < V; g++) {
+        if (walls[g] != 3) continue;
+        int p[3];
+        s_pos(c, g, p);
+        p[0] -= 1;
+        const long src = s_index(c, p);
+        n[g] = n[src];
+        for (int d = 0; d < D; d++) u[g + d * V] = u[src + d * V];
+        for (int q = 0; q < Q; q++) pop[g + q * V] = pop[src + q * V];
+    }
+}
+
+static void s_collide(const orc_simple *c, long V, double *pop, double *u, const double *n, const double *psi,
+                      const int *walls) {
+    const int D = c->dim, Q = c->Q;
+    const double om = c->omega;
+    for (long g = 0; g < V; g++) {
+        if (c->gravity ? walls[g] == 0 : walls[g] != 1) continue;
+        int pos[3], np[3];
+        s_pos(c, g, pos);
+        double F[3] = {0., 0., 0.}, lu_post[3] = {0., 0., 0.};
+        const double lpsi = psi[g];
+        for (int a = 0; a < c->QE; a++) {
+            for (int d = 0; d < D; d++) np[d] = ((pos[d] + c->e[d + a * D] + c->L[d]) % c->L[d]);
+            const double npsi = psi[s_index(c, np)];
+            for (int d = 0; d < D; d++) F[d] += c->e[d + a * D] * c->we[a] * npsi;
+        }
+        for (int d = 0; d < D; d++) F[d] *= -c->G * lpsi;
+        if (c->gravity) F[1] += c->g;
+        const double ln = n[g];
+        double lu[3];
+        if (c->forcing == 0) {
+            for (int d = 0; d < D; d++) {
+                lu[d] = u[g + V * d] + 0.5 * F[d] / ln;
+                u[g + V * d] = lu[d];
+            }
+            double u_dot_u = 0., F_dot_u = 0.;
+            for (int d = 0; d < D; d++) {
+                u_dot_u += lu[d] * lu[d];
+                F_dot_u += F[d] * lu[d];
+            }
+            for (int q = 0; q < Q; q++) {
+                double u_dot_xi = 0., F_dot_xi = 0.;
+                for (int d = 0; d < D; d++) {
+                    u_dot_xi += lu[d] * c->xi[d + q * D];
+                    F_dot_xi += F[d] * c->xi[d + q * D];
+                }
+                double leq = 1., lguo = 0.;
+                leq += +u_dot_xi * 3.0 + 0.5 * u_dot_xi * u_dot_xi * 9.0;
+                leq += -0.5 * u_dot_u * 3.0;
+                leq = leq * ln * c->w[q];
+                lguo += +F_dot_xi * 3.0 + F_dot_xi * u_dot_xi * 9.0;
+                lguo += -F_dot_u * 3.0;
+                lguo = lguo * c->w[q];
+                pop[g + q * V] = pop[g + q * V] * (1. - om) + leq * om + (1. - 0.5 * om) * lguo;
+            }
+        } else {
+            for (int d = 0; d < D; d++) lu[d] = u[g + V * d] + F[d] / ln / om;
+            double u_dot_u = 0.;
+            for (int d = 0; d < D; d++) u_dot_u += lu[d] * lu[d];
+            for (int q = 0; q < Q; q++) {
+                double u_dot_xi = 0.;
+                for (int d = 0; d < D; d++) u_dot_xi += lu[d] * c->xi[d + q * D];
+                double leq = 1.;
+                leq += +u_dot_xi * 3.0 + 0.5 * u_dot_xi * u_dot_xi * 9.0;
+                leq += -0.5 * u_dot_u * 3.0;
+                leq = leq * ln * c->w[q];
+                pop[g + q * V] = pop[g + q * V] * (1. - om) + leq * om;
+                for (int d = 0; d < D; d++) lu_post[d] += pop[g + q * V] * c->xi[d + q * D];
+            }
+            for (int d = 0; d < D; d++) u[g + V * d] = 0.5 * (u[g + V * d] + lu_post[d] / ln);
+        }
+    }
+}
+
+static void s_moments_psi(const orc_simple *c, long V, const double *cur, double *n, double *u, double *psi,
+                          const int *walls) {
+    const int D = c->dim, Q = c->Q;
+    for (long g = 0; g < V; g++) {  /* moments */
+        if (walls[g] != 1) continue;
+        double lu[3] = {0., 0., 0.}, ln = 0.;
+        for (int q = 0; q < Q; q++) {
+            const double lpop = cur[g + q * V];
+            ln += lpop;
+            for (int d = 0; d < D; d++) lu[d] += lpop * c->xi[d + q * D];
+        }
+        n[g] = ln;
+        for (int d = 0; d < D; d++) u[g + d * V] = lu[d] / ln;
+    }
+    for (long g = 0; g < V; g++)  /* psi */
+        if (walls[g]) psi[g] = psi_of(c->psi_kind, n[g]);
+}
+
+static void s_stream_bounce(const orc_simple *c, long V, const double *cur, double *nxt, const int *walls) {
+    const int D = c->dim, Q = c->Q;
+    for (long g = 0; g < V; g++) {  /* pull stream */
+        int dp[3], sp[3];
+        s_pos(c, g, dp);
+        nxt[g] = cur[g];
+        for (int q = 1; q < Q; q++) {
+            for (int d = 0; d < D; d++) sp[d] = ((dp[d] - c->xi[d + q * D] + c->L[d]) % c->L[d]);
+            nxt[g + q * V] = cur[s_index(c, sp) + q * V];
+        }
+    }
+    for (long g = 0; g < V; g++) {  /* halfway bounce-back out of the walls */
+        if (walls[g] != 0) continue;
+        int sp[3], dp[3];
+        s_pos(c, g, sp);
+        nxt[g] = 0.;
+        for (int q = 1; q < Q; q++) {
+            const int qd = c->opposite[q];
+            for (int d = 0; d < D; d++) dp[d] = ((sp[d] + c->xi[d + qd * D] + c->L[d]) % c->L[d]);
+            nxt[s_index(c, dp) + qd * V] = nxt[g + q * V];
+            nxt[g + q * V] = 0.;
+        }
+    }
+}
+
+int orc_simple_run(const orc_simple *c, double *pop_a, double *pop_b, double *n, double *u, double *psi,
+                   const int *walls, int nsteps, int *swapped) {
+    long V = 1;
+    for (int d = 0; d < c->dim; d++) V *= c->L[d];
+    double *cur = pop_a, *nxt = pop_b;
+    for (int s = 0; s < nsteps; s++) {
+        if (c->order == 1) {
+            s_outlet(c, V, cur, n, u, walls);
+            s_inlet(c, V, cur, n, u, walls);
+            s_stream_bounce(c, V, cur, nxt, walls);
+            double *t = cur; cur = nxt; nxt = t;
+            s_moments_psi(c, V, cur, n, u, psi, walls);
+            s_collide(c, V, cur, u, n, psi, walls);
+            continue;
+        }
+        if (c->inout) {
+            s_inlet(c, V, cur, n, u, walls);
+            s_outlet(c, V, cur, n, u, walls);
+        }
+        s_moments_psi(c, V, cur, n, u, psi, walls);
+        s_collide(c, V, cur, u, n, psi, walls);
+        s_stream_bounce(c, V, cur, nxt, walls);
+        double *t = cur; cur = nxt; nxt = t;
+    }
+    *swapped = (cur != pop_a);
+    return 0;
+}
