@@ -43,6 +43,8 @@ struct FusedShape {
     static constexpr int SMEM = (RING * HC + 2 * STAGE) * 4;  // psi ring + double-buffered stage
     // fluctuating step: plus each thread's random moments of its current cell
     static constexpr int NSMEM = SMEM + (L::Q - D - 1) * NT * 4;
+    // walls: plus a ring of the halo planes' wall flags (bytes)
+    static constexpr int WSMEM = SMEM + (RING * HC + 3) / 4 * 4;
 };
 
 __device__ __forceinline__ void cp_async4(float *smem, const float *gmem) {
@@ -102,18 +104,27 @@ __device__ __forceinline__ float bgk_fp32(const float *f, const float *u, const 
 // populations of a cell (the lattice volume, or a batch's total volume).
 // ST (not void): the fluctuating step (noise.cuh), generator states of type ST
 // at seeds[s*V + cell].
-template <class L, class S, bool MRT, class ST = void>
+// WALLS: wall flags (1 fluid, 0 wall; other values neither) and the psi the
+// walls keep, as k_density_psi_walls + k_fcs_walls: n and psi of fluid cells
+// only, the walls' psi elsewhere; non-fluid cells pass their populations on
+// unchanged; a population pushed into a wall cell goes to the opposite
+// population of its own cell (halfway bounce-back).  The halo planes' flags sit
+// in a shared-memory ring beside the psi ring.
+template <class L, class S, bool MRT, class ST = void, bool WALLS = false>
 __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float *__restrict__ pop_out, const int V,
                                            const int Lx, const int Ly, const int Lz, const int x0, const int y0,
                                            const int m0, const int m1, const float neg_g, const float rho0,
                                            const StepParams<L, S, float> &p, float *smem,
-                                           ST *seeds = nullptr, const NoiseParams<L, float> *z = nullptr) {
+                                           ST *seeds = nullptr, const NoiseParams<L, float> *z = nullptr,
+                                           const unsigned char *__restrict__ walls = nullptr,
+                                           const float *__restrict__ psi_w = nullptr) {
     constexpr bool NOISE = !std::is_void<ST>::value;
     using SeedT = typename std::conditional<NOISE, ST, int>::type;
     using SH = FusedShape<L, S>;
     constexpr int D = L::D, Q = L::Q, R = SH::R, HX = SH::HX, HC = SH::HC, NT = SH::NT, RING = SH::RING;
     float *ring = smem;  // psi ring [RING][HC], then (2D) 2 stage buffers [HPT][Q][NT]
     float *stage0 = smem + RING * HC;
+    unsigned char *fring = reinterpret_cast<unsigned char *>(smem + RING * HC + 2 * SH::STAGE);  // WALLS
     const int tid = threadIdx.x;
     const int Lm = D == 3 ? Lz : Ly;       // marching extent
     const int PL = D == 3 ? Lx * Ly : Lx;  // cells per plane
@@ -159,7 +170,16 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
             float s = v[k][lex_q<Q>(0)];
 #pragma unroll
             for (int i = 1; i < Q; i++) s += v[k][lex_q<Q>(i)];
-            if (k + 1 < SH::HPT || c < HC) slot[c] = psi_fast(p.psi_kind, rho0 + s);
+            if (k + 1 < SH::HPT || c < HC) {
+                float ps = psi_fast(p.psi_kind, rho0 + s);
+                if constexpr (WALLS) {
+                    const int cell = poff + hoff[k];
+                    const unsigned char fl = walls[cell];
+                    fring[wrapm(m, RING) * HC + c] = fl;
+                    if (fl != 1) ps = psi_w[cell];
+                }
+                slot[c] = ps;
+            }
         }
     };
     // asynchronous copy of this thread's halo populations of plane m into a stage buffer
@@ -181,6 +201,7 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
     auto stage_reduce = [&](int m) {
         const float *st = stage0 + (m & 1) * SH::STAGE;
         float *slot = ring + wrapm(m, RING) * HC;
+        const int poff = wrapm(m, Lm) * PL;
 #pragma unroll
         for (int k = 0; k < SH::HPT; k++) {
             const int c = tid + k * NT;
@@ -188,7 +209,14 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
                 float s = st[(k * Q + lex_q<Q>(0)) * NT + tid];
 #pragma unroll
                 for (int i = 1; i < Q; i++) s += st[(k * Q + lex_q<Q>(i)) * NT + tid];
-                slot[c] = psi_fast(p.psi_kind, rho0 + s);
+                float ps = psi_fast(p.psi_kind, rho0 + s);
+                if constexpr (WALLS) {
+                    const int cell = poff + hoff[k];
+                    const unsigned char fl = walls[cell];
+                    fring[wrapm(m, RING) * HC + c] = fl;
+                    if (fl != 1) ps = psi_w[cell];
+                }
+                slot[c] = ps;
             }
         }
     };
@@ -233,6 +261,15 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
             const float *sb[RING];
 #pragma unroll
             for (int k = 0; k < RING; k++) sb[k] = ring + wrapm(m + k - R, RING) * HC + ty * HX + tx;
+            // flags of planes m-1, m, m+1 at this thread's halo position
+            const unsigned char *fb[3] = {nullptr, nullptr, nullptr};
+            bool fluid = true;  // a non-fluid cell passes its populations on unchanged
+            if constexpr (WALLS) {
+#pragma unroll
+                for (int o = 0; o < 3; o++)
+                    fb[o] = fring + wrapm(m + o - 1, RING) * HC + ty * HX + tx + (D == 3 ? R * HX : 0) + R;
+                fluid = fb[1][0] == 1;
+            }
             // random moments of the cell into this thread's shared-memory slot
             // (the states die here; the collision reads the moments back)
             float *rms = smem + SH::RING * SH::HC + 2 * SH::STAGE + tid;
@@ -243,6 +280,10 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
 #pragma unroll
                 for (int k = 0; k < NR; k++) rms[k * NT] = rm[k];
             }
+            if (!fluid) {
+#pragma unroll
+                for (int q = 0; q < Q; q++) pop_out[g + q * V] = f[q];
+            } else {
             float d = f[lex_q<Q>(0)];
 #pragma unroll
             for (int i = 1; i < Q; i++) d += f[lex_q<Q>(i)];
@@ -287,10 +328,18 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
                 // (at omega = 1 it is a plain multiply), so the rest population
                 // balances exactly the rounded values that are stored
                 rest_pop = __fsub_rn(rest_pop, out);
-                const int dst = X3[L::xi(q, 0) + 1] + Y3[L::xi(q, 1) + 1] + Z3[L::xi(q, D - 1) + 1];
-                pop_out[dst + q * V] = out;
+                int dst = X3[L::xi(q, 0) + 1] + Y3[L::xi(q, 1) + 1] + Z3[L::xi(q, D - 1) + 1];
+                int qd = q;
+                if constexpr (WALLS) {
+                    if (fb[L::xi(q, D - 1) + 1][(D == 3 ? L::xi(q, 1) * HX : 0) + L::xi(q, 0)] == 0) {
+                        dst = g;
+                        qd = opposite_q<L>(q);
+                    }
+                }
+                pop_out[dst + qd * V] = out;
             }
             pop_out[g] = rest_pop;
+            }
         }
     }
 }
@@ -314,6 +363,29 @@ __global__ void __launch_bounds__(FusedShape<L, S>::NT, MRT ? 2 : 3)
         const int m0 = ic * fg.chunk;
         fused_tile<L, S, MRT>(pop, pop_out, (int)fg.V, fg.L[0], fg.L[1], fg.L[2], ix * SH::TX, iy * SH::TY, m0,
                               min(m0 + fg.chunk, Lm), p.neg_g, p.rho0, p, smem);
+    }
+}
+
+// walls (BGK): the halo flags and walls' psi cost a few registers more, so two
+// CTAs per SM
+template <class L, class S>
+__global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
+    k_fused_walls(const float *__restrict__ pop, float *__restrict__ pop_out,
+                  const __grid_constant__ StepParams<L, S, float> p, const FusedGeom fg,
+                  const unsigned char *__restrict__ walls, const float *__restrict__ psi_w) {
+    using SH = FusedShape<L, S>;
+    constexpr int D = L::D;
+    extern __shared__ float smem[];
+    const int Lm = D == 3 ? fg.L[2] : fg.L[1];
+    for (int item = blockIdx.x; item < fg.items; item += gridDim.x) {
+        const int ix = item % fg.tiles_x;
+        const int rest = item / fg.tiles_x;
+        const int iy = D == 3 ? rest % fg.tiles_y : 0;
+        const int ic = D == 3 ? rest / fg.tiles_y : rest;
+        const int m0 = ic * fg.chunk;
+        fused_tile<L, S, false, void, true>(pop, pop_out, (int)fg.V, fg.L[0], fg.L[1], fg.L[2], ix * SH::TX,
+                                            iy * SH::TY, m0, min(m0 + fg.chunk, Lm), p.neg_g, p.rho0, p, smem,
+                                            nullptr, nullptr, walls, psi_w);
     }
 }
 

@@ -84,6 +84,10 @@ struct KernelOps {
                                void *seeds, const void *noise_params, int grid, cudaStream_t st);
     int (*fused_noise_occupancy)();
     unsigned (*noise_mask)(int q);  // nonzero pattern the single-pass noise kernel assumes
+    // single-pass step with walls (FP32 BGK only, else null)
+    cudaError_t (*fused_walls)(const void *pop, void *pop_out, const void *step_params, const FusedGeom &fg,
+                               const unsigned char *walls, const void *psi_w, int grid, cudaStream_t st);
+    int (*fused_walls_occupancy)();
     // the "simple" step family (FP64 only, else null)
     cudaError_t (*simple_inlet)(void *pop, void *dn, void *u, const unsigned char *walls, const SimpleParams &p,
                                 int grid, cudaStream_t st);
@@ -357,6 +361,39 @@ struct Ops {
         return b > 0 ? b : 1;
     }
     static constexpr bool F64 = std::is_same<Real, double>::value;
+    static void allow_smem_walls() {
+        if constexpr (std::is_same<Real, float>::value && !MRT) {
+            static bool done[64] = {};  // per device
+            int dev = 0;
+            cudaGetDevice(&dev);
+            if (dev < 0 || dev >= 64 || !done[dev]) {
+                cudaFuncSetAttribute(k_fused_walls<L, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     FusedShape<L, S>::WSMEM);
+                if (dev >= 0 && dev < 64) done[dev] = true;
+            }
+        }
+    }
+    static cudaError_t fused_walls(const void *pop, void *pop_out, const void *sp, const FusedGeom &fg,
+                                   const unsigned char *walls, const void *psi_w, int grid, cudaStream_t st) {
+        if constexpr (std::is_same<Real, float>::value && !MRT) {
+            using SH = FusedShape<L, S>;
+            allow_smem_walls();
+            k_fused_walls<L, S><<<grid, SH::NT, SH::WSMEM, st>>>((const float *)pop, (float *)pop_out,
+                                                                 *static_cast<const SP *>(sp), fg, walls,
+                                                                 (const float *)psi_w);
+            return cudaGetLastError();
+        }
+        return cudaErrorNotSupported;
+    }
+    static int fused_walls_occupancy() {
+        int b = 0;
+        if constexpr (std::is_same<Real, float>::value && !MRT) {
+            using SH = FusedShape<L, S>;
+            allow_smem_walls();
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fused_walls<L, S>, SH::NT, SH::WSMEM);
+        }
+        return b > 0 ? b : 1;
+    }
     static cudaError_t simple_inlet(void *pop, void *dn, void *u, const unsigned char *walls, const SimpleParams &sp,
                                     int grid, cudaStream_t st) {
         if constexpr (F64) {
@@ -419,6 +456,7 @@ struct Ops {
                                     sizeof(NP), MRT ? nullptr : &fill_noise, MRT ? nullptr : &fcs_noise,
                                     &noise_occupancy, (f32 && !MRT) ? &fused_noise : nullptr,
                                     &fused_noise_occupancy, &NoiseMask<L>::m,
+                                    (f32 && !MRT) ? &fused_walls : nullptr, &fused_walls_occupancy,
                                     F64 ? &simple_inlet : nullptr, F64 ? &simple_outlet : nullptr,
                                     F64 ? &simple_moments : nullptr, F64 ? &simple_collide : nullptr,
                                     F64 ? &simple_stream : nullptr};

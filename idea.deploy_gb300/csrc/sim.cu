@@ -335,8 +335,8 @@ int stencil_order(int D, const int *e, int qe) {
 bool fused_fits(const sclbm_sim *s) { return (int64_t)s->Q * s->V < ((int64_t)1 << 31); }
 
 bool fused_path(const sclbm_sim *s) {
-    return s->ops->fused != nullptr && s->path != SCLBM_PATH_TWO_PASS && fused_fits(s) && !s->walls &&
-           !s->simple_mode &&
+    return s->ops->fused != nullptr && s->path != SCLBM_PATH_TWO_PASS && fused_fits(s) &&
+           (!s->walls || s->ops->fused_walls != nullptr) && !s->simple_mode &&
            (!s->noise_kind || (s->ops->fused_noise != nullptr && !s->noise_indep && s->noise_sparse &&
                                (int64_t)s->noise_streams * s->V < ((int64_t)1 << 31)));
 }
@@ -403,7 +403,10 @@ int launch_step(sclbm_sim *s, cudaEvent_t *ev = nullptr) {
     cudaError_t e;
     if (s->simple_mode) return launch_simple(s, ev);
     if (fused_path(s)) {
-        if (s->noise_kind)
+        if (s->walls)
+            e = o->fused_walls(s->pop[s->cur], s->pop[s->cur ^ 1], s->sp.data(), s->fg, s->walls, s->psi_w,
+                               s->fused_grid, s->st);
+        else if (s->noise_kind)
             e = o->fused_noise(s->pop[s->cur], s->pop[s->cur ^ 1], s->sp.data(), s->fg, s->seeds, s->np.data(),
                                s->fused_grid, s->st);
         else
@@ -439,7 +442,9 @@ void plan_fused(sclbm_sim *s) {
     g.tiles_x = (s->L[0] + o->fused_tx - 1) / o->fused_tx;
     g.tiles_y = s->D == 3 ? (s->L[1] + o->fused_ty - 1) / o->fused_ty : 1;
     const int Lm = s->D == 3 ? s->L[2] : s->L[1];
-    const int resident = s->sms * (s->noise_kind ? o->fused_noise_occupancy() : o->fused_occupancy());
+    const int resident = s->sms * (s->noise_kind ? o->fused_noise_occupancy()
+                                   : s->walls    ? o->fused_walls_occupancy()
+                                                 : o->fused_occupancy());
     const int base = g.tiles_x * g.tiles_y;
     int best_c = 1;
     double best = -1;
@@ -1166,6 +1171,7 @@ int sclbm_set_walls(sclbm_sim *s, const int *walls, const double *psi) {
     for (auto &g : s->graph)
         if (g) cudaGraphExecDestroy(g), g = nullptr;  // the step's kernels change
     s->moments_fresh = s->dn_fresh = false;
+    plan_fused(s);  // the single pass with walls has its own occupancy
     return SCLBM_OK;
 }
 

@@ -88,3 +88,29 @@ def test_dropin_getwalls_mainloopwalls():
     if pop is not None:
         assert rel_err(pop[:, fluid], z['pop_100'][:, fluid]) < 1e-12
     sc.End()
+
+
+@pytest.mark.parametrize('name', CASES)
+def test_fp32_single_pass_with_walls(name):
+    """FP32 walls in one pass (k_fused_walls: flags and the walls' psi in the
+    halo reduction, bounce-back from a shared-memory flag ring) against the
+    FP32 two-pass kernels (k_density_psi_walls + k_fcs_walls) and the FP64
+    reference run: same populations to FP32 rounding of the two collision
+    forms, mass conserved to FP32 rounding, FP64's density within 1e-3."""
+    z, c = load(name)
+    steps = int(z['steps'][-1])
+    fluid = (z['walls'] == 1).ravel()
+    out = []
+    for path in (_lib.PATH_FUSED, _lib.PATH_TWO_PASS):
+        s = start(z, c, precision=_lib.FP32_SHIFTED, rho0=0.2)
+        s.set_tuning(path)
+        assert s.kernels_per_step() == (1 if path == _lib.PATH_FUSED else 2)
+        m0, _ = s.reductions()
+        s.step(steps)
+        m1, _ = s.reductions()
+        assert abs(m1 - m0) / m0 < 1e-5, (name, path)
+        out.append((s.get_populations().reshape(z['pop_init'].shape[0], -1)[:, fluid], s.get_density()[fluid]))
+        s.close()
+    assert rel_err(out[0][0], out[1][0]) < 1e-4, rel_err(out[0][0], out[1][0])
+    want = z['pop_%d' % steps].reshape(z['pop_init'].shape[0], -1)[:, fluid].sum(0)
+    assert rel_err(out[0][1], want) < 1e-3
