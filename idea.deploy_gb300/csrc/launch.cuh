@@ -396,52 +396,53 @@ struct Ops {
     }
     static cudaError_t simple_inlet(void *pop, void *dn, void *u, const unsigned char *walls, const SimpleParams &sp,
                                     int grid, cudaStream_t st) {
-        if constexpr (F64) {
+        if constexpr (F64)
             k_simple_inlet<L, STRICT><<<grid, 256, 0, st>>>((double *)pop, (double *)dn, (double *)u, walls, sp);
-            return cudaGetLastError();
-        }
-        return cudaErrorNotSupported;
+        else
+            k_simple_inlet_f32<L><<<grid, 256, 0, st>>>((float *)pop, (float *)dn, (float *)u, walls, sp);
+        return cudaGetLastError();
     }
     static cudaError_t simple_outlet(void *pop, void *dn, void *u, const unsigned char *walls, const SimpleParams &sp,
                                      int grid, cudaStream_t st) {
-        if constexpr (F64) {
-            k_simple_outlet<L><<<grid, 256, 0, st>>>((double *)pop, (double *)dn, (double *)u, walls, sp);
-            return cudaGetLastError();
-        }
-        return cudaErrorNotSupported;
+        k_simple_outlet<L, Real><<<grid, 256, 0, st>>>((Real *)pop, (Real *)dn, (Real *)u, walls, sp);
+        return cudaGetLastError();
     }
     static cudaError_t simple_moments(const void *pop, void *dn, void *u, void *psi, const unsigned char *walls,
                                       const SimpleParams &sp, int grid, cudaStream_t st) {
-        if constexpr (F64) {
+        if constexpr (F64)
             k_simple_moments<L, STRICT><<<grid, 256, 0, st>>>((const double *)pop, (double *)dn, (double *)u,
                                                               (double *)psi, walls, sp);
-            return cudaGetLastError();
-        }
-        return cudaErrorNotSupported;
+        else
+            k_simple_moments_f32<L><<<grid, 256, 0, st>>>((const float *)pop, (float *)dn, (float *)u, (float *)psi,
+                                                          walls, sp);
+        return cudaGetLastError();
     }
     static cudaError_t simple_collide(int sc, int push, const void *pop, void *pop_out, const void *dn, void *u,
                                       const void *psi, const unsigned char *walls, const SimpleParams &sp, int grid,
                                       cudaStream_t st) {
+        const Real *a = (const Real *)pop, *n = (const Real *)dn, *ps = (const Real *)psi;
+        Real *b = (Real *)pop_out, *uu = (Real *)u;
         if constexpr (F64) {
-            const double *a = (const double *)pop, *n = (const double *)dn, *ps = (const double *)psi;
-            double *b = (double *)pop_out, *uu = (double *)u;
             if (!sc)
                 k_simple_collide<L, S, STRICT, false, true><<<grid, 128, 0, st>>>(a, b, n, uu, ps, walls, sp);
             else if (push)
                 k_simple_collide<L, S, STRICT, true, true><<<grid, 128, 0, st>>>(a, b, n, uu, ps, walls, sp);
             else
                 k_simple_collide<L, S, STRICT, true, false><<<grid, 128, 0, st>>>(a, b, n, uu, ps, walls, sp);
-            return cudaGetLastError();
+        } else {
+            if (!sc)
+                k_simple_collide_f32<L, S, false, true><<<grid, 128, 0, st>>>(a, b, n, uu, ps, walls, sp);
+            else if (push)
+                k_simple_collide_f32<L, S, true, true><<<grid, 128, 0, st>>>(a, b, n, uu, ps, walls, sp);
+            else
+                k_simple_collide_f32<L, S, true, false><<<grid, 128, 0, st>>>(a, b, n, uu, ps, walls, sp);
         }
-        return cudaErrorNotSupported;
+        return cudaGetLastError();
     }
     static cudaError_t simple_stream(const void *pop, void *pop_out, const unsigned char *walls, const SimpleParams &sp,
                                      int grid, cudaStream_t st) {
-        if constexpr (F64) {
-            k_simple_stream<L><<<grid, 128, 0, st>>>((const double *)pop, (double *)pop_out, walls, sp);
-            return cudaGetLastError();
-        }
-        return cudaErrorNotSupported;
+        k_simple_stream<L, Real><<<grid, 128, 0, st>>>((const Real *)pop, (Real *)pop_out, walls, sp);
+        return cudaGetLastError();
     }
     static const KernelOps *ops() {
         constexpr bool f32 = std::is_same<Real, float>::value;
@@ -457,9 +458,8 @@ struct Ops {
                                     &noise_occupancy, (f32 && !MRT) ? &fused_noise : nullptr,
                                     &fused_noise_occupancy, &NoiseMask<L>::m,
                                     (f32 && !MRT) ? &fused_walls : nullptr, &fused_walls_occupancy,
-                                    F64 ? &simple_inlet : nullptr, F64 ? &simple_outlet : nullptr,
-                                    F64 ? &simple_moments : nullptr, F64 ? &simple_collide : nullptr,
-                                    F64 ? &simple_stream : nullptr};
+                                    &simple_inlet, &simple_outlet, &simple_moments, &simple_collide,
+                                    &simple_stream};
         return &o;
     }
 };

@@ -1317,7 +1317,7 @@ int sclbm_set_simple(sclbm_sim *s, int forcing, int use_walls, int gravity, doub
         return SCLBM_OK;
     }
     if (forcing != SCLBM_SIMPLE_GUO && forcing != SCLBM_SIMPLE_SC) return fail(SCLBM_ERR_ARG, "forcing %d", forcing);
-    if (s->fp32 || !s->ops->simple_collide) return fail(SCLBM_ERR_UNSUPPORTED, "the simple step family is FP64");
+    if (!s->ops->simple_collide) return fail(SCLBM_ERR_UNSUPPORTED, "no simple-step kernels");
     if (s->mrt) return fail(SCLBM_ERR_UNSUPPORTED, "the simple step family is BGK");
     if (s->noise_kind) return fail(SCLBM_ERR_UNSUPPORTED, "the simple step family with fluctuations");
     if (gravity && forcing != SCLBM_SIMPLE_GUO)
@@ -1345,6 +1345,7 @@ int sclbm_set_simple(sclbm_sim *s, int forcing, int use_walls, int gravity, doub
     p.g = g;
     p.u_in = u_in;
     p.psi_kind = s->psi_kind;
+    p.rho0 = s->fp32 ? s->rho0 : 0.0;
     p.gravity = gravity ? 1 : 0;
     s->simple_mode = forcing;
     s->simple_inout = inlet_outlet ? 1 : 0;

@@ -23,6 +23,12 @@
 // are never read).  STRICT keeps every operation of the reference's C in its
 // order (__dmul_rn / __dadd_rn, no contraction).  Wall flags may be null (the
 // periodic loops): every cell is fluid.
+//
+// FP32 (the *_f32 kernels): the library's shifted storage, g_q = f_q - w_q rho0
+// and dn = n - rho0, with the same formulas regrouped around the deviations
+// (f_eq - w rho0 = w [dn + n (3 u.xi + 4.5 (u.xi)^2 - 1.5 u^2)]) and the rest
+// population from mass conservation, as the other FP32 kernels; not a parity
+// path (the FP64 kernels are).
 #pragma once
 
 #include "kernels.cuh"
@@ -37,6 +43,7 @@ struct SimpleParams {
     double omega;
     double g;          // gravity along y
     double u_in;       // inlet velocity along x
+    double rho0;       // FP32: the storage shift (0 in FP64)
     int psi_kind;
     int gravity;       // 1: F_y += g, collide every cell with walls != 0
 };
@@ -93,9 +100,9 @@ __global__ void __launch_bounds__(256) k_simple_inlet(double *__restrict__ pop, 
 }
 
 // outlet (walls == 3): copy of the cell at x - 1
-template <class L>
-__global__ void __launch_bounds__(256) k_simple_outlet(double *__restrict__ pop, double *__restrict__ dn,
-                                                      double *__restrict__ u, const unsigned char *__restrict__ walls,
+template <class L, class Real>
+__global__ void __launch_bounds__(256) k_simple_outlet(Real *__restrict__ pop, Real *__restrict__ dn,
+                                                      Real *__restrict__ u, const unsigned char *__restrict__ walls,
                                                       const SimpleParams p) {
     constexpr int D = L::D, Q = L::Q;
     const int64_t V = p.geo.V;
@@ -258,8 +265,8 @@ __global__ void __launch_bounds__(128) k_simple_collide(const double *pop, doubl
 
 // pure push stream with halfway bounce-back (the SC inlet/outlet loop streams
 // before it collides)
-template <class L>
-__global__ void __launch_bounds__(128) k_simple_stream(const double *__restrict__ pop, double *__restrict__ pop_out,
+template <class L, class Real>
+__global__ void __launch_bounds__(128) k_simple_stream(const Real *__restrict__ pop, Real *__restrict__ pop_out,
                                                       const unsigned char *__restrict__ walls, const SimpleParams p) {
     constexpr int D = L::D, Q = L::Q;
     const int64_t V = p.geo.V;
@@ -276,6 +283,160 @@ __global__ void __launch_bounds__(128) k_simple_stream(const double *__restrict_
                 qd = opposite_q<L>(q);
             }
             pop_out[(int64_t)qd * V + dst] = pop[(int64_t)q * V + g];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// FP32-shifted kernels
+// ---------------------------------------------------------------------------
+template <class L>
+__global__ void __launch_bounds__(256) k_simple_inlet_f32(float *__restrict__ pop, float *__restrict__ dn,
+                                                         float *__restrict__ u, const unsigned char *__restrict__ walls,
+                                                         const SimpleParams p) {
+    constexpr int D = L::D, Q = L::Q;
+    const int64_t V = p.geo.V;
+    const float rho0 = (float)p.rho0, us = (float)p.u_in;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < V; g += (int64_t)gridDim.x * blockDim.x) {
+        if (flag_of(walls, g) != 2) continue;
+        const float n = 2.0f, dnv = (float)(2.0 - p.rho0);
+        dn[g] = dnv;
+        u[g] = us;
+#pragma unroll
+        for (int d = 1; d < D; d++) u[(int64_t)d * V + g] = 0.0f;
+        const float u2 = us * us;
+#pragma unroll
+        for (int q = 0; q < Q; q++) {
+            const float ux = us * (float)L::xi(q, 0);
+            pop[(int64_t)q * V + g] = (float)p.w[q] * (dnv + n * (3.0f * ux + 4.5f * ux * ux - 1.5f * u2));
+        }
+        (void)rho0;
+    }
+}
+
+template <class L>
+__global__ void __launch_bounds__(256) k_simple_moments_f32(const float *__restrict__ pop, float *__restrict__ dn,
+                                                           float *__restrict__ u, float *__restrict__ psi,
+                                                           const unsigned char *__restrict__ walls,
+                                                           const SimpleParams p) {
+    constexpr int D = L::D, Q = L::Q;
+    const int64_t V = p.geo.V;
+    const float rho0 = (float)p.rho0;
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < V; g += (int64_t)gridDim.x * blockDim.x) {
+        const int fl = flag_of(walls, g);
+        if (fl == 0) continue;
+        if (fl == 1) {
+            float sdn = 0.0f, lu[D];
+#pragma unroll
+            for (int d = 0; d < D; d++) lu[d] = 0.0f;
+#pragma unroll
+            for (int q = 0; q < Q; q++) {
+                const float f = pop[(int64_t)q * V + g];
+                sdn += f;
+#pragma unroll
+                for (int d = 0; d < D; d++)
+                    if (L::xi(q, d) != 0) lu[d] += L::xi(q, d) > 0 ? f : -f;
+            }
+            dn[g] = sdn;
+            const float n = rho0 + sdn;
+#pragma unroll
+            for (int d = 0; d < D; d++) u[(int64_t)d * V + g] = lu[d] / n;
+        }
+        psi[g] = psi_of<float>(p.psi_kind, rho0 + dn[g]);
+    }
+}
+
+template <class L, class S, bool SC, bool PUSH>
+__global__ void __launch_bounds__(128) k_simple_collide_f32(const float *pop, float *pop_out,
+                                                           const float *__restrict__ dn, float *__restrict__ u,
+                                                           const float *__restrict__ psi,
+                                                           const unsigned char *__restrict__ walls,
+                                                           const SimpleParams p) {
+    constexpr int D = L::D, Q = L::Q;
+    const int64_t V = p.geo.V;
+    const float om = (float)p.omega, rho0 = (float)p.rho0, neg_g = (float)p.neg_g;
+    const float a1 = (float)(1.0 - p.omega), a2 = (float)(1.0 - 0.5 * p.omega);
+    for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < V; g += (int64_t)gridDim.x * blockDim.x) {
+        const int fl = flag_of(walls, g);
+        if (fl == 0) continue;
+        Cell<D> c;
+        cell_of<D>(g, p.geo.L, c);
+        float f[Q];
+#pragma unroll
+        for (int q = 0; q < Q; q++) f[q] = pop[(int64_t)q * V + g];
+        const bool collide = p.gravity ? true : fl == 1;
+        if (collide) {
+            float F[D];
+#pragma unroll
+            for (int d = 0; d < D; d++) F[d] = 0.0f;
+#pragma unroll
+            for (int a = 0; a < S::QE; a++) {
+                const int64_t nb = index_at<D>(c, S::e(a, 0), S::e(a, 1), D == 3 ? S::e(a, 2) : 0, p.geo.L);
+                const float npsi = psi[nb];
+#pragma unroll
+                for (int d = 0; d < D; d++)
+                    if (S::e(a, d) != 0) F[d] = fmaf((float)(S::e(a, d) * p.we[a]), npsi, F[d]);
+            }
+            const float sc = neg_g * psi[g];
+#pragma unroll
+            for (int d = 0; d < D; d++) F[d] *= sc;
+            if (p.gravity) F[1] += (float)p.g;
+            const float dnv = dn[g], n = rho0 + dnv;
+            float lu[D], u0[D];
+#pragma unroll
+            for (int d = 0; d < D; d++) u0[d] = u[(int64_t)d * V + g];
+            float rest = dnv, up[D];
+#pragma unroll
+            for (int d = 0; d < D; d++) {
+                lu[d] = SC ? u0[d] + F[d] / n / om : u0[d] + 0.5f * F[d] / n;
+                if (!SC) u[(int64_t)d * V + g] = lu[d];
+                up[d] = 0.0f;
+            }
+            float u2 = 0.0f, uF = 0.0f;
+#pragma unroll
+            for (int d = 0; d < D; d++) {
+                u2 = fmaf(lu[d], lu[d], u2);
+                uF = fmaf(F[d], lu[d], uF);
+            }
+#pragma unroll
+            for (int q = 1; q < Q; q++) {
+                float ux = 0.0f, Fx = 0.0f;
+#pragma unroll
+                for (int d = 0; d < D; d++)
+                    if (L::xi(q, d) != 0) {
+                        ux += L::xi(q, d) > 0 ? lu[d] : -lu[d];
+                        Fx += L::xi(q, d) > 0 ? F[d] : -F[d];
+                    }
+                const float wq = (float)p.w[q];
+                const float eqd = wq * (dnv + n * (3.0f * ux + 4.5f * ux * ux - 1.5f * u2));
+                float out = fmaf(f[q], a1, om * eqd);
+                if (!SC) out = fmaf(a2, wq * (3.0f * Fx + 9.0f * Fx * ux - 3.0f * uF), out);
+                f[q] = out;
+                rest = __fsub_rn(rest, out);
+#pragma unroll
+                for (int d = 0; d < D; d++)
+                    if (L::xi(q, d) != 0) up[d] += L::xi(q, d) > 0 ? out : -out;
+            }
+            f[0] = rest;  // the collision conserves mass
+            if (SC) {
+#pragma unroll
+                for (int d = 0; d < D; d++) u[(int64_t)d * V + g] = 0.5f * (u0[d] + up[d] / n);
+            }
+        }
+        if constexpr (PUSH) {
+#pragma unroll
+            for (int q = 0; q < Q; q++) {
+                int64_t dst = index_at<D>(c, L::xi(q, 0), L::xi(q, 1), D == 3 ? L::xi(q, 2) : 0, p.geo.L);
+                int qd = q;
+                if (q != 0 && flag_of(walls, dst) == 0) {
+                    dst = g;
+                    qd = opposite_q<L>(q);
+                }
+                pop_out[(int64_t)qd * V + dst] = f[q];
+            }
+        } else if (collide) {
+#pragma unroll
+            for (int q = 0; q < Q; q++) pop_out[(int64_t)q * V + g] = f[q];
         }
     }
 }

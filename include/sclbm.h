@@ -173,8 +173,9 @@ SCLBM_API int sclbm_set_walls(sclbm_sim *s, const int *walls, const double *psi)
  * adds g to F_y and collides every non-wall cell (Guo only).  inlet_outlet != 0:
  * wall flags 2 (inlet: n = 2, u = (u_in, 0, ..), equilibrium) and 3 (outlet: the
  * cell at x - 1) are set each step; with SCLBM_SIMPLE_SC the step then streams
- * before it collides, as the reference's loop does.  FP64 only (its arithmetic,
- * in the reference's order with SCLBM_LIT_ROUND15).  After steps of this family
+ * before it collides, as the reference's loop does.  FP64: the reference's
+ * arithmetic in its order (with SCLBM_LIT_ROUND15); FP32_SHIFTED: the same
+ * formulas on the shifted storage, mass-conserving.  After steps of this family
  * the density and velocity read back are the arrays the reference's loops leave
  * (the moments at the start of the last step, the stored velocity).
  * use_walls = 0: every cell fluid (MainLoopSimple[SC], which ignore walls).

@@ -3,7 +3,8 @@ MainLoopSimple* loops) against the reference's own runs
 (tests/golden/simple_*.npz): FP64 in the reference's operation order;
 populations, density, velocity and psi on every non-wall cell within 1e-12
 (relative, max-norm; psi uses CUDA's exp, which may differ from glibc's by an
-ulp) after every recorded step count."""
+ulp) after every recorded step count.  FP32-shifted within 1e-3 of the
+reference, mass-conserving."""
 import numpy as np
 import pytest
 
@@ -83,14 +84,40 @@ def test_dropin_simple_loops(name):
 def test_simple_refusals():
     z, c = load('walls_guo_d2e4')
     x, f = XIStencils[c['xi']], FStencils[c['fs']]
-    s = _lib.Sim(2, c['dims'], x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], c['G'], precision=_lib.FP32_SHIFTED,
-                 rho0=0.2)
-    with pytest.raises(_lib.SclbmError):
-        s.set_simple(_lib.SIMPLE_GUO)               # FP64 only
-    s.close()
     s = _lib.Sim(2, c['dims'], x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], c['G'])
     with pytest.raises(_lib.SclbmError):
         s.set_simple(_lib.SIMPLE_GUO, use_walls=True)   # no walls yet
     with pytest.raises(_lib.SclbmError):
         s.set_simple(_lib.SIMPLE_SC, gravity=1e-5)      # gravity goes with Guo
+    s.close()
+
+
+@pytest.mark.parametrize('name', CASES)
+def test_simple_fp32_follows_reference(name):
+    """The FP32-shifted simple kernels (the same formulas on g = f - w rho0,
+    rest population from mass conservation): density within 1e-3 of the
+    reference's FP64 run on every non-wall cell at the last checkpoint; total
+    mass conserved to FP32 rounding where the loop has no inlet/outlet."""
+    z, c = load(name)
+    x, f = XIStencils[c['xi']], FStencils[c['fs']]
+    D = len(c['dims'])
+    s = _lib.Sim(D, c['dims'], x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], c['G'], tau=c['tau'],
+                 precision=_lib.FP32_SHIFTED, rho0=float(z['n_init'].min()))
+    has_walls = 'walls' in z.files
+    if has_walls:
+        s.set_walls(z['walls'], z['psi_w'])
+    s.set_populations(z['pop_init'])
+    s.set_density(z['n_init'])
+    s.set_velocity(np.zeros(D * s.V))
+    forcing, g, u_in = kind(c)
+    s.set_simple(_lib.SIMPLE_SC if forcing == 'sc' else _lib.SIMPLE_GUO, use_walls=has_walls, gravity=g,
+                 inlet_outlet=u_in is not None, u_in=u_in or 0.0)
+    m0, _ = s.reductions()
+    k = int(z['steps'][-1])
+    s.step(k)
+    live = (z['walls'] != 0).ravel() if has_walls else np.ones(s.V, bool)
+    assert rel_err(s.get_density()[live], z['n_%d' % k].ravel()[live]) < 1e-3, name
+    if u_in is None:
+        m1, _ = s.reductions()
+        assert abs(m1 - m0) / m0 < 1e-5, name
     s.close()
