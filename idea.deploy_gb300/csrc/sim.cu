@@ -255,6 +255,8 @@ struct sclbm_sim {
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
     int64_t device_bytes = 0;
     void *stage = nullptr;  // pinned host staging buffer (lazy)
+    int transfer = SCLBM_TRANSFER_AUTO;
+    bool pageable_access = false;  // the device reads and writes pageable host memory (coherent C2C)
     cudaEvent_t stage_ev[2] = {nullptr, nullptr};
 };
 
@@ -527,7 +529,61 @@ inline double shift_at(const double *plane_shift, int64_t i, int64_t plane) {
     return plane_shift ? plane_shift[i / plane] : 0.0;
 }
 
+// Direct transfers: a kernel reads or writes the caller's FP64 host array itself
+// (over NVLink-C2C on Grace-Blackwell) and converts on the fly, with the same
+// per-element arithmetic as the staged path (x - shift rounded once to Real;
+// (double)x + shift), so both give identical arrays.  Used when the host
+// array is pinned / registered memory, or when the device reports access to
+// pageable host memory; otherwise the staged path runs.
+struct ShiftTab {
+    double v[27];
+    int64_t plane;
+};
+
+template <class Real>
+__global__ void __launch_bounds__(256) k_from_host(Real *__restrict__ dst, const double *__restrict__ src, int64_t count,
+                                                   const ShiftTab sh) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = (Real)(src[i] - sh.v[i / sh.plane]);
+}
+
+template <class Real>
+__global__ void __launch_bounds__(256) k_to_host(double *__restrict__ dst, const Real *__restrict__ src, int64_t count,
+                                                 const ShiftTab sh) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < count; i += (int64_t)gridDim.x * blockDim.x)
+        dst[i] = (double)src[i] + sh.v[i / sh.plane];
+}
+
+// device-usable address of a host array for the direct path, or null
+const void *direct_address(sclbm_sim *s, const void *host, int64_t count, int64_t plane) {
+    if (s->transfer == SCLBM_TRANSFER_STAGED || plane <= 0 || (count + plane - 1) / plane > 27) return nullptr;
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, host) == cudaSuccess && a.type == cudaMemoryTypeHost)
+        return a.devicePointer ? a.devicePointer : host;
+    cudaGetLastError();
+    return s->pageable_access ? host : nullptr;
+}
+
+bool fill_shift(ShiftTab &sh, const double *plane_shift, int64_t count, int64_t plane) {
+    sh.plane = plane;
+    const int64_t np = (count + plane - 1) / plane;
+    for (int64_t k = 0; k < 27; k++) sh.v[k] = (plane_shift && k < np) ? plane_shift[k] : 0.0;
+    return true;
+}
+
 int d2h_real(sclbm_sim *s, const void *src, double *dst, int64_t count, const double *plane_shift, int64_t plane) {
+    if (count <= 0) return SCLBM_OK;
+    if (void *d = (void *)direct_address(s, dst, count, plane)) {
+        ShiftTab sh;
+        fill_shift(sh, plane_shift, count, plane);
+        const int grid = s->sms * 8;
+        if (s->fp32) k_to_host<float><<<grid, 256, 0, s->st>>>((double *)d, (const float *)src, count, sh);
+        else k_to_host<double><<<grid, 256, 0, s->st>>>((double *)d, (const double *)src, count, sh);
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaStreamSynchronize(s->st));
+        return SCLBM_OK;
+    }
+    if (s->transfer == SCLBM_TRANSFER_DIRECT) return fail(SCLBM_ERR_UNSUPPORTED, "host array not device-accessible");
     int rc = ensure_stage(s);
     if (rc) return rc;
     const int64_t per = (int64_t)(STAGE_BYTES / 2 / s->rs);
@@ -557,6 +613,18 @@ int d2h_real(sclbm_sim *s, const void *src, double *dst, int64_t count, const do
 }
 
 int h2d_real(sclbm_sim *s, void *dst, const double *src, int64_t count, const double *plane_shift, int64_t plane) {
+    if (count <= 0) return SCLBM_OK;
+    if (const void *d = direct_address(s, src, count, plane)) {
+        ShiftTab sh;
+        fill_shift(sh, plane_shift, count, plane);
+        const int grid = s->sms * 8;
+        if (s->fp32) k_from_host<float><<<grid, 256, 0, s->st>>>((float *)dst, (const double *)d, count, sh);
+        else k_from_host<double><<<grid, 256, 0, s->st>>>((double *)dst, (const double *)d, count, sh);
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaStreamSynchronize(s->st));
+        return SCLBM_OK;
+    }
+    if (s->transfer == SCLBM_TRANSFER_DIRECT) return fail(SCLBM_ERR_UNSUPPORTED, "host array not device-accessible");
     int rc = ensure_stage(s);
     if (rc) return rc;
     const int64_t per = (int64_t)(STAGE_BYTES / 2 / s->rs);
@@ -798,6 +866,12 @@ int sclbm_create(const sclbm_params *p, sclbm_sim **out) {
     s->psi_kind = p->psi_kind;
     s->literals = p->literals;
     s->sms = prop.multiProcessorCount;
+    {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, p->device) != cudaSuccess) v = 0;
+        cudaGetLastError();
+        s->pageable_access = v == 1;
+    }
     s->w.assign(p->w, p->w + p->q);
     s->we.assign(p->we, p->we + p->qe);
     s->xi.assign(p->xi, p->xi + p->q * p->dim);
@@ -1350,6 +1424,15 @@ int sclbm_set_simple(sclbm_sim *s, int forcing, int use_walls, int gravity, doub
     s->simple_mode = forcing;
     s->simple_inout = inlet_outlet ? 1 : 0;
     s->simple_walls = use_walls ? 1 : 0;
+    return SCLBM_OK;
+}
+
+int sclbm_set_transfer(sclbm_sim *s, int mode, int *pageable_access) {
+    if (!s) return fail(SCLBM_ERR_ARG, "null handle");
+    if (mode != SCLBM_TRANSFER_AUTO && mode != SCLBM_TRANSFER_STAGED && mode != SCLBM_TRANSFER_DIRECT)
+        return fail(SCLBM_ERR_ARG, "transfer mode %d", mode);
+    s->transfer = mode;
+    if (pageable_access) *pageable_access = s->pageable_access ? 1 : 0;
     return SCLBM_OK;
 }
 

@@ -21,6 +21,7 @@ CRNG_NONE, CRNG_MINSTD, CRNG_NUMREC, CRNG_MMIX = 0, 1, 2, 3
 CRNG_KINDS = {'MINSTD': CRNG_MINSTD, 'NUMREC': CRNG_NUMREC, 'MMIX': CRNG_MMIX}
 SEEDS_STREAM_MAJOR, SEEDS_CELL_MAJOR = 0, 1
 SIMPLE_OFF, SIMPLE_GUO, SIMPLE_SC = 0, 1, 2
+TRANSFER_AUTO, TRANSFER_STAGED, TRANSFER_DIRECT = 0, 1, 2
 
 
 class SclbmError(RuntimeError):
@@ -106,6 +107,7 @@ SIGNATURES = {
     'sclbm_set_fluctuations': [_P, ctypes.c_int, ctypes.c_int, _D, _D, _P, ctypes.c_int, _P, _P],
     'sclbm_get_seeds': [_P, _P, ctypes.c_int],
     'sclbm_set_simple': [_P, ctypes.c_int, ctypes.c_int, ctypes.c_int, _D, ctypes.c_int, _D],
+    'sclbm_set_transfer': [_P, ctypes.c_int, _IP],
     'sclbm_mlp_param_count': [_IP],
     'sclbm_mlp_create': [ctypes.c_int, ctypes.c_uint64, ctypes.POINTER(_P)],
     'sclbm_mlp_destroy': [_P],
@@ -366,6 +368,13 @@ class Sim:
         inlet / outlet wall flags 2 / 3 with inlet velocity u_in."""
         call('sclbm_set_simple', self.h, int(forcing), int(bool(use_walls)), int(gravity is not None),
              float(gravity or 0.0), int(bool(inlet_outlet)), float(u_in))
+
+    def set_transfer(self, mode):
+        """TRANSFER_AUTO / _STAGED / _DIRECT; returns whether the device can
+        access pageable host memory."""
+        pa = ctypes.c_int()
+        call('sclbm_set_transfer', self.h, int(mode), ctypes.byref(pa))
+        return bool(pa.value)
 
     def restore_mass(self, target=float('nan')):
         """FP64 mass before; if target is finite, restore it (rest populations)."""

@@ -223,6 +223,18 @@ SCLBM_API int sclbm_set_fluctuations(sclbm_sim *s, int generator, int indep, dou
 /* the current generator states (crng.sims_idpy_memory['seeds'].D2H()) */
 SCLBM_API int sclbm_get_seeds(sclbm_sim *s, void *seeds, int layout);
 
+/* host <-> device transfers of the FP64 field arrays: SCLBM_TRANSFER_AUTO
+ * (default) lets a kernel read / write the caller's array directly (converting
+ * on the fly) when it is pinned or registered memory or the device can access
+ * pageable host memory (Grace-Blackwell NVLink-C2C), else copies through a
+ * pinned staging buffer; _STAGED always stages; _DIRECT fails on an array the
+ * device cannot access.  Both paths give identical arrays.  pageable_access
+ * (optional) reports the device's pageable-memory access. */
+#define SCLBM_TRANSFER_AUTO   0
+#define SCLBM_TRANSFER_STAGED 1
+#define SCLBM_TRANSFER_DIRECT 2
+SCLBM_API int sclbm_set_transfer(sclbm_sim *s, int mode, int *pageable_access);
+
 /* time stepping: enqueue nsteps steps on the handle's stream (returns without
  * waiting); sclbm_sync waits for everything enqueued on the handle */
 SCLBM_API int sclbm_step(sclbm_sim *s, int64_t nsteps);
