@@ -482,8 +482,12 @@ class ShanChenMultiPhase:
         self.init_status['n'] = True
         self.init_status['u'] = True
 
-    def GetDensityField(self):
-        return self._sim.get_density().reshape(self._flip())
+    def GetDensityField(self, out=None):
+        """The density field (shape flip(dim_sizes)).  out: an optional
+        float64 array of V values to read into (e.g. pinned memory reused
+        across calls); the result is then a view of it."""
+        flat = None if out is None else np.asarray(out).reshape(-1)
+        return self._sim.get_density(flat).reshape(self._flip())
 
     def GetVelocityField(self):
         u = self._sim.get_velocity()

@@ -195,6 +195,9 @@ class Sim:
         h = ctypes.c_void_p()
         call('sclbm_create', ctypes.byref(p), ctypes.byref(h))
         self.h = h
+        pa = ctypes.c_int()
+        call('sclbm_set_transfer', self.h, TRANSFER_AUTO, ctypes.byref(pa))
+        self._direct = bool(pa.value)   # read-backs go straight into (pageable) host arrays
 
     def _arr(self, a):
         if a is None:
@@ -225,18 +228,29 @@ class Sim:
         assert u.size == self.V * self.dim
         call('sclbm_set_velocity', self.h, ptr(u))
 
-    def get_density(self):
-        out = np.empty(self.V)
+    def _out(self, out, n):
+        if out is None:
+            out = np.empty(n)
+            if self._direct:
+                # fault the pages in on the CPU (much faster than the device
+                # faulting them in over the link on its first write)
+                out.fill(0.0)
+            return out
+        assert out.dtype == np.float64 and out.size == n and out.flags['C_CONTIGUOUS']
+        return out
+
+    def get_density(self, out=None):
+        out = self._out(out, self.V)
         call('sclbm_get_density', self.h, ptr(out))
         return out
 
-    def get_velocity(self):
-        out = np.empty(self.V * self.dim)
+    def get_velocity(self, out=None):
+        out = self._out(out, self.V * self.dim)
         call('sclbm_get_velocity', self.h, ptr(out))
         return out
 
-    def get_populations(self):
-        out = np.empty(self.V * self.q)
+    def get_populations(self, out=None):
+        out = self._out(out, self.V * self.q)
         call('sclbm_get_populations', self.h, ptr(out))
         return out
 
@@ -374,6 +388,7 @@ class Sim:
         access pageable host memory."""
         pa = ctypes.c_int()
         call('sclbm_set_transfer', self.h, int(mode), ctypes.byref(pa))
+        self._direct = bool(pa.value) and int(mode) != TRANSFER_STAGED
         return bool(pa.value)
 
     def restore_mass(self, target=float('nan')):
