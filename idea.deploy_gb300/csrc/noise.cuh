@@ -237,10 +237,11 @@ __device__ __forceinline__ void add_noise(const NoiseParams<L, Real> &z, const R
         add_noise_terms<NR, Real, STRICT>(z.coef[q], rm, out[q], std::make_integer_sequence<int, NR>{});
 }
 
-// four CTAs of 128 threads per SM (at most 128 registers a thread): the
-// batched generator-state loads would otherwise take the whole register file
+// FP32: four CTAs of 128 threads per SM (at most 128 registers a thread), or
+// the batched generator-state loads would take the whole register file; FP64
+// (bound by the FP64 rate, not by occupancy): two, so nothing spills
 template <class L, class S, class Real, bool STRICT, class T>
-__global__ void __launch_bounds__(128, 4) k_fcs_noise(const Real *__restrict__ pop, Real *__restrict__ pop_out,
+__global__ void __launch_bounds__(128, std::is_same<Real, float>::value ? 4 : 2) k_fcs_noise(const Real *__restrict__ pop, Real *__restrict__ pop_out,
                                                   const Real *__restrict__ dn, const Real *__restrict__ psi,
                                                   T *__restrict__ seeds,
                                                   const __grid_constant__ StepParams<L, S, Real> p,
