@@ -349,10 +349,11 @@ def run_ours(a, dist):
                    'collision': 'MRT (rates 1.0)', 'precision': 'FP32 deviations from w_q*rho0, FP64 reductions',
                    'l2': 'inputs larger than L2 (populations 2 x %.2f GB)' % (Q * 4 * V / 1e9),
                    'parallelism': 'replicas x%d' % dist.ws if dist.ws > 1 else 'single GPU'},
-        'step_path': {'path': 'single pass (k_fused)' if path == 2 else 'two passes (k_density_psi + k_fcs)',
+        'step_path': {'path': 'single pass (k_fused, paired halo loads)' if path == 3 else
+                      'single pass (k_fused)' if path == 2 else 'two passes (k_density_psi + k_fcs)',
                       'chunk_planes': chunk, 'grid': grid,
                       'collision_kernel': 'MRT with all rates 1.0 is exactly BGK with omega=1: sparse BGK operator'},
-        'roofline': {'bound': 'hbm', 'kernel': 'k_fused (single pass)' if path == 2 else
+        'roofline': {'bound': 'hbm', 'kernel': 'k_fused (single pass)' if path in (2, 3) else
                      'k_fcs (force+collide+push-stream pass)',
                      'achieved': round(ach, 1), 'peak': hbm, 'unit': 'GB/s', 'frac': round(ach / hbm, 4),
                      'peak_source': 'MEASURED_PEAKS.json hbm_gbs (measured copy)' if pk else 'fallback 6.8 TB/s',

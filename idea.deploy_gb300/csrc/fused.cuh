@@ -62,6 +62,7 @@ struct FusedGeom {
     int64_t V;
     int tiles_x, tiles_y, chunks, chunk;  // work decomposition
     int items;
+    int pairs;  // 3D, even Lx and even halo radius: halo populations loaded two cells per load
 };
 
 // FP32 pseudopotential with the fast hardware exp2/reciprocal (relative error
@@ -110,7 +111,15 @@ __device__ __forceinline__ float bgk_fp32(const float *f, const float *u, const 
 // unchanged; a population pushed into a wall cell goes to the opposite
 // population of its own cell (halfway bounce-back).  The halo planes' flags sit
 // in a shared-memory ring beside the psi ring.
-template <class L, class S, bool MRT, class ST = void, bool WALLS = false>
+// PAIRS (3D, even radius R, even Lx): the halo reduction loads each
+// population of two x-adjacent cells with one 8-byte load.  The halo row is
+// TX + 2R cells wide and starts at an even x, so a row is (TX + 2R)/2 whole
+// pairs that never straddle the periodic wrap; one thread reduces one pair
+// ((TX/2 + R) * (TY + 2R) <= NT pairs per plane), which halves the halo load
+// and address instructions of the scalar form (two cells per thread, the
+// second re-read by threads that have none).  The sums run in the same order,
+// so the results are bit-identical to the scalar form.
+template <class L, class S, bool MRT, class ST = void, bool WALLS = false, bool PAIRS = false>
 __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float *__restrict__ pop_out, const int V,
                                            const int Lx, const int Ly, const int Lz, const int x0, const int y0,
                                            const int m0, const int m1, const float neg_g, const float rho0,
@@ -139,6 +148,14 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
         const int gx = wrapm(x0 - R + hx, Lx);
         hoff[k] = D == 3 ? gx + Lx * wrapm(y0 - R + hy, Ly) : gx;
     }
+    // PAIRS: in-plane offset of the (even) first cell of this thread's halo pair
+    constexpr int HP = HX / 2, NPAIR = HP * SH::HY;
+    static_assert(!PAIRS || (D == 3 && R % 2 == 0 && NPAIR <= NT && !WALLS), "paired halo loads");
+    int hoffp = 0;
+    if constexpr (PAIRS) {
+        const int c = tid < NPAIR ? tid : 0;
+        hoffp = wrapm(x0 - R + 2 * (c % HP), Lx) + Lx * wrapm(y0 - R + c / HP, Ly);
+    }
     // interior cell of this thread and its wrapped neighbour columns / rows
     const int x = x0 + tx, y = D == 3 ? y0 + ty : 0;
     const bool in_tile = x < Lx && (D == 2 || y < Ly);
@@ -156,6 +173,24 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
     auto psi_plane = [&](int m) {
         float *slot = ring + wrapm(m, RING) * HC;
         const int poff = wrapm(m, Lm) * PL;
+        if constexpr (PAIRS) {
+            // halo cell c = 2*tid and 2*tid+1 of the plane (HX = 2*HP)
+            if (tid < NPAIR) {
+                const float2 *src = reinterpret_cast<const float2 *>(pop + (poff + hoffp));
+                const int V2 = V >> 1;
+                float2 w[Q];
+#pragma unroll
+                for (int q = 0; q < Q; q++) w[q] = __ldg(src + q * V2);
+                float sx = w[lex_q<Q>(0)].x, sy = w[lex_q<Q>(0)].y;
+#pragma unroll
+                for (int i = 1; i < Q; i++) {
+                    sx += w[lex_q<Q>(i)].x;
+                    sy += w[lex_q<Q>(i)].y;
+                }
+                reinterpret_cast<float2 *>(slot)[tid] =
+                    make_float2(psi_fast(p.psi_kind, rho0 + sx), psi_fast(p.psi_kind, rho0 + sy));
+            }
+        } else {
         float v[SH::HPT][Q];
 #pragma unroll
         for (int k = 0; k < SH::HPT; k++) {
@@ -180,6 +215,7 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
                 }
                 slot[c] = ps;
             }
+        }
         }
     };
     // asynchronous copy of this thread's halo populations of plane m into a stage buffer
@@ -347,7 +383,7 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
 // Three CTAs per SM for BGK (80 registers, no spills; 5% faster than two at
 // 256^3 D3Q19 E6, measured in one run), two for the dense MRT operator and
 // for the fluctuating step.
-template <class L, class S, bool MRT>
+template <class L, class S, bool MRT, bool PAIRS = false>
 __global__ void __launch_bounds__(FusedShape<L, S>::NT, MRT ? 2 : 3)
     k_fused(const float *__restrict__ pop, float *__restrict__ pop_out, const __grid_constant__ StepParams<L, S, float> p,
             const FusedGeom fg) {
@@ -361,8 +397,8 @@ __global__ void __launch_bounds__(FusedShape<L, S>::NT, MRT ? 2 : 3)
         const int iy = D == 3 ? rest % fg.tiles_y : 0;
         const int ic = D == 3 ? rest / fg.tiles_y : rest;
         const int m0 = ic * fg.chunk;
-        fused_tile<L, S, MRT>(pop, pop_out, (int)fg.V, fg.L[0], fg.L[1], fg.L[2], ix * SH::TX, iy * SH::TY, m0,
-                              min(m0 + fg.chunk, Lm), p.neg_g, p.rho0, p, smem);
+        fused_tile<L, S, MRT, void, false, PAIRS>(pop, pop_out, (int)fg.V, fg.L[0], fg.L[1], fg.L[2], ix * SH::TX,
+                                                  iy * SH::TY, m0, min(m0 + fg.chunk, Lm), p.neg_g, p.rho0, p, smem);
     }
 }
 

@@ -194,6 +194,13 @@ struct Ops {
         if constexpr (std::is_same<Real, float>::value) {
             using SH = FusedShape<L, S>;
             allow_smem();
+            if constexpr (L::D == 3 && S::R % 2 == 0) {
+                if (fg.pairs) {
+                    k_fused<L, S, MRT, true><<<grid, SH::NT, SH::SMEM, st>>>((const float *)pop, (float *)pop_out,
+                                                                             *static_cast<const SP *>(sp), fg);
+                    return cudaGetLastError();
+                }
+            }
             k_fused<L, S, MRT><<<grid, SH::NT, SH::SMEM, st>>>((const float *)pop, (float *)pop_out,
                                                                *static_cast<const SP *>(sp), fg);
             return cudaGetLastError();
@@ -209,6 +216,9 @@ struct Ops {
             if (dev < 0 || dev >= 64 || !done[dev]) {
                 cudaFuncSetAttribute(k_fused<L, S, MRT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      FusedShape<L, S>::SMEM);
+                if constexpr (L::D == 3 && S::R % 2 == 0)
+                    cudaFuncSetAttribute(k_fused<L, S, MRT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         FusedShape<L, S>::SMEM);
                 if (dev >= 0 && dev < 64) done[dev] = true;
             }
         }
@@ -219,6 +229,11 @@ struct Ops {
             allow_smem();
             int b = 0;
             cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fused<L, S, MRT>, SH::NT, SH::SMEM);
+            if constexpr (L::D == 3 && S::R % 2 == 0) {
+                int bp = 0;
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bp, k_fused<L, S, MRT, true>, SH::NT, SH::SMEM);
+                if (bp > 0 && bp < b) b = bp;
+            }
             return b > 0 ? b : 1;
         }
         return 0;

@@ -13,7 +13,7 @@ from . import build as _build
 
 OK, ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA, ERR_STATE, ERR_NOMEM, ERR_NODEVICE = range(7)
 PSI_EXP_INV, PSI_ONE_MINUS_EXP, PSI_IDENTITY = 0, 1, 2
-PATH_AUTO, PATH_TWO_PASS, PATH_FUSED = 0, 1, 2
+PATH_AUTO, PATH_TWO_PASS, PATH_FUSED, PATH_FUSED_PAIRS = 0, 1, 2, 3
 COLL_BGK, COLL_MRT = 0, 1
 FP64, FP32_SHIFTED = 0, 1
 LIT_ROUND15, LIT_EXACT = 0, 1

@@ -250,9 +250,12 @@ SCLBM_API int sclbm_profile_step(sclbm_sim *s, int64_t nsteps, double *ms, int n
 SCLBM_API int sclbm_kernels_per_step(const sclbm_sim *s, int *count);
 
 /* step path: AUTO = single pass where built (FP32-shifted), else two passes */
-#define SCLBM_PATH_AUTO     0
+#define SCLBM_PATH_AUTO     0  /* the one pass where it applies (paired halo loads where they apply) */
 #define SCLBM_PATH_TWO_PASS 1  /* density+psi pass, then force+collide+stream pass */
-#define SCLBM_PATH_FUSED    2  /* one pass, psi recomputed in a shared-memory halo ring */
+#define SCLBM_PATH_FUSED    2  /* one pass, psi recomputed in a shared-memory halo ring, one halo cell per load */
+/* the one pass with the halo populations loaded two x-adjacent cells per load
+ * (3D lattices with even Lx and an E6/E8 stencil; otherwise as SCLBM_PATH_FUSED) */
+#define SCLBM_PATH_FUSED_PAIRS 3
 /* choose the step path and the marching chunk (planes per work item, 0 = planned) */
 SCLBM_API int sclbm_set_tuning(sclbm_sim *s, int path, int chunk);
 SCLBM_API int sclbm_get_tuning(const sclbm_sim *s, int *path, int *chunk, int *grid);

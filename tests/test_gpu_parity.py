@@ -365,7 +365,7 @@ def test_single_pass_fp32_close_to_fp64_short():
     a = _lib.Sim(3, dims, x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], -4.5)
     b = _lib.Sim(3, dims, x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], -4.5, precision=_lib.FP32_SHIFTED,
                  rho0=float(n0.mean()))
-    assert b.get_tuning()[0] == _lib.PATH_FUSED and b.kernels_per_step() == 1
+    assert b.get_tuning()[0] == _lib.PATH_FUSED_PAIRS and b.kernels_per_step() == 1
     for s in (a, b):
         s.set_density(n0)
         s.set_velocity(np.zeros(3 * s.V))
@@ -400,3 +400,31 @@ def test_density_readers_follow_the_single_pass_kernel():
     idx = [0, 1234, s.V - 1]
     np.testing.assert_allclose(s.density_at(idx), n_pop[idx], rtol=1e-6)
     s.close()
+
+
+@pytest.mark.parametrize('st,dims', [('D3E6', (40, 24, 36)), ('D3E8', (32, 32, 24)), ('D3E6', (66, 18, 20)),
+                                     ('D3E6', (35, 16, 12))])
+@pytest.mark.parametrize('coll', ['bgk', 'mrt'])
+def test_single_pass_paired_halo_loads_bit_identical(st, dims, coll):
+    """Paired halo loads (two x-adjacent cells per 8-byte load) sum in the same
+    order as the scalar single pass, so the populations are bit-identical;
+    partial tiles in x and y, and an odd Lx (35: the scalar form runs)."""
+    x, f = XIStencils['D3Q19'], FStencils[st]
+    Q = 19
+    rates = np.array([1.0, 1.0, 1.0] + [1.1 + 0.02 * i for i in range(Q - 3)])
+    kw = dict(collision=_lib.COLL_MRT, mrt_s=np.diag(rates)) if coll == 'mrt' else dict(tau=0.9)
+    n0 = droplet(dims, min(dims) / 4, 4.5, 0.2, 2.0, 23)
+    pops = []
+    for path in (_lib.PATH_FUSED, _lib.PATH_FUSED_PAIRS):
+        s = _lib.Sim(3, dims, x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], -4.5, precision=_lib.FP32_SHIFTED,
+                     rho0=1.0, **kw)
+        s.set_tuning(path, 5)
+        want = path if dims[0] % 2 == 0 else _lib.PATH_FUSED
+        assert s.get_tuning()[0] == want
+        s.set_density(n0)
+        s.set_velocity(np.zeros(3 * s.V))
+        s.init_populations()
+        s.step(6)
+        pops.append(s.get_populations())
+        s.close()
+    assert np.array_equal(pops[0], pops[1])
