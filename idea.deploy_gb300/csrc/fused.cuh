@@ -83,9 +83,14 @@ __device__ __forceinline__ int wrapm(int x, int L) {
 // eu = xi_q.u, eF = xi_q.F, C0 = w dn - 1.5 w n u^2 - 3 (1-w/2) u.F,
 // a = 4.5 w n, b = 3 w n, c = 9 (1-w/2), d = 3 (1-w/2); the same operator as
 // the expanded form (2nd-order Hermite equilibrium + Guo term, Collisions.py:163-185).
+// A direction q and its opposite qb (eu and eF change sign) are made together:
+// with t = a eu^2 + c eu eF (even in xi) and s = b eu + d eF (odd in xi),
+//   g*_q = (1-w) g_q + w_q (C0 + t + s),  g*_qb = (1-w) g_qb + w_qb (C0 + t - s),
+// so eu, eF, t and C0 + t are computed once for the two.
 template <class L, class S>
-__device__ __forceinline__ float bgk_fp32(const float *f, const float *u, const float *F, int q,
-                                          const StepParams<L, S, float> &p, float C0, float a, float b) {
+__device__ __forceinline__ void bgk_pair_fp32(const float *f, const float *u, const float *F, int q, int qb,
+                                              const StepParams<L, S, float> &p, float C0, float a, float b,
+                                              float &out_q, float &out_qb) {
     constexpr int D = L::D;
     float eu = 0.f, eF = 0.f;
 #pragma unroll
@@ -93,11 +98,34 @@ __device__ __forceinline__ float bgk_fp32(const float *f, const float *u, const 
         if (L::xi(q, c) > 0) { eu += u[c]; eF += F[c]; }
         if (L::xi(q, c) < 0) { eu -= u[c]; eF -= F[c]; }
     }
-    float t = fmaf(a, eu, b);
-    t = fmaf(p.fc, eF, t);
-    t = fmaf(eu, t, p.fd * eF);
-    const float rhs = p.wq[q] * (C0 + t);
-    return p.a_nonzero ? fmaf(p.A[q][q], f[q], rhs) : rhs;
+    const float even = eu * fmaf(a, eu, p.fc * eF);
+    const float odd = fmaf(b, eu, p.fd * eF);
+    const float base = C0 + even;
+    const float rq = p.wq[q] * (base + odd), rqb = p.wq[qb] * (base - odd);
+    out_q = p.a_nonzero ? fmaf(p.A[q][q], f[q], rq) : rq;
+    out_qb = p.a_nonzero ? fmaf(p.A[qb][qb], f[qb], rqb) : rqb;
+}
+
+// index of the force-stencil vector opposite to e_a, from a table the
+// compiler builds once per stencil (a search per unrolled use would not fold)
+template <class S>
+struct OppositeE {
+    int v[S::QE];
+    constexpr OppositeE() : v() {
+        for (int a = 0; a < S::QE; a++) {
+            v[a] = a;
+            for (int k = 0; k < S::QE; k++) {
+                bool same = true;
+                for (int d = 0; d < S::D; d++) same = same && (S::e(k, d) == -S::e(a, d));
+                if (same) v[a] = k;
+            }
+        }
+    }
+};
+template <class S>
+SCLBM_HD constexpr int opposite_e(int a) {
+    constexpr OppositeE<S> t{};
+    return t.v[a];
 }
 
 // One work item: the tile (x0, y0) of one lattice, planes [m0, m1).  pop and
@@ -323,18 +351,24 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
             float d = f[lex_q<Q>(0)];
 #pragma unroll
             for (int i = 1; i < Q; i++) d += f[lex_q<Q>(i)];
-            // Shan-Chen force from the psi ring (compile-time offsets)
+            // Shan-Chen force from the psi ring (compile-time offsets); the
+            // stencil is symmetric (w_a = w_-a, checked on the host), so each
+            // pair +-e_a contributes w_a e_a (psi(x+e_a) - psi(x-e_a))
             float F[D];
 #pragma unroll
             for (int c = 0; c < D; c++) F[c] = 0.f;
-#pragma unroll
-            for (int a = 0; a < S::QE; a++) {
+            auto psi_at = [&](int a) {
                 const int em = D == 3 ? S::e(a, 2) : S::e(a, 1);
                 const int ey = D == 3 ? S::e(a, 1) : 0;
-                const float ps = sb[em + R][(D == 3 ? (R + ey) * HX : 0) + R + S::e(a, 0)];
+                return sb[em + R][(D == 3 ? (R + ey) * HX : 0) + R + S::e(a, 0)];
+            };
+#pragma unroll
+            for (int a = 0; a < S::QE; a++) {
+                if (opposite_e<S>(a) < a) continue;
+                const float dps = psi_at(a) - psi_at(opposite_e<S>(a));
 #pragma unroll
                 for (int c = 0; c < D; c++)
-                    if (S::e(a, c) != 0) F[c] = fmaf(p.sw[a][c], ps, F[c]);
+                    if (S::e(a, c) != 0) F[c] = fmaf(p.sw[a][c], dps, F[c]);
             }
             const float sc = neg_g * sb[R][(D == 3 ? R * HX : 0) + R];
 #pragma unroll
@@ -352,11 +386,17 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
             const float C0 = p.omega * d - p.om15 * n * u2 - p.fd * uF;
             const float a = p.om45 * n, b = p.om3 * n;
             float rest_pop = d;
+            float pend[Q];  // BGK: a direction's result computed with its opposite's
 #pragma unroll
             for (int q = 1; q < Q; q++) {
                 float out;
-                if (MRT) collide_cell<L, S, true, float, false>(f, d, n, u, F, q, p, out);
-                else out = bgk_fp32<L, S>(f, u, F, q, p, C0, a, b);
+                if (MRT) {
+                    collide_cell<L, S, true, float, false>(f, d, n, u, F, q, p, out);
+                } else {
+                    if (opposite_q<L>(q) > q) bgk_pair_fp32<L, S>(f, u, F, q, opposite_q<L>(q), p, C0, a, b, out,
+                                                                  pend[opposite_q<L>(q)]);
+                    else out = pend[q];
+                }
                 if constexpr (NOISE)
                     add_noise_terms_strided<NR, NT>(NoiseMask<L>::m(q), z->coef[q], rms, out,
                                                     std::make_integer_sequence<int, NR>{});

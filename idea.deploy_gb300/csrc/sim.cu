@@ -244,6 +244,7 @@ struct sclbm_sim {
     double tau_bgk = 1.0;           // BGK relaxation time of the current operator
     // the "simple" step family (sclbm_set_simple): 0 off, SCLBM_SIMPLE_GUO / _SC
     int simple_mode = 0, simple_inout = 0, simple_walls = 0;
+    bool sym_weights = true;  // opposite directions / stencil vectors carry equal weights
     SimpleParams spar = {};
     double *red = nullptr;
     int red_blocks = 0;
@@ -333,11 +334,30 @@ int stencil_order(int D, const int *e, int qe) {
     return 0;
 }
 
+// the single-pass kernels pair every lattice direction and force-stencil vector
+// with its opposite and assume equal weights for the two (true of the D2Q9 /
+// D3Q19 lattices and the isotropic E4-E8 stencils)
+bool weights_symmetric(const sclbm_params *p) {
+    auto sym = [&](const int *v, const double *w, int n) {
+        for (int a = 0; a < n; a++) {
+            int b = -1;
+            for (int k = 0; k < n && b < 0; k++) {
+                bool opp = true;
+                for (int d = 0; d < p->dim; d++) opp = opp && v[k * p->dim + d] == -v[a * p->dim + d];
+                if (opp) b = k;
+            }
+            if (b < 0 || w[a] != w[b]) return false;
+        }
+        return true;
+    };
+    return sym(p->xi, p->w, p->q) && sym(p->e, p->we, p->qe);
+}
+
 // the single-pass kernel indexes populations with 32-bit offsets (q*V + cell)
 bool fused_fits(const sclbm_sim *s) { return (int64_t)s->Q * s->V < ((int64_t)1 << 31); }
 
 bool fused_path(const sclbm_sim *s) {
-    return s->ops->fused != nullptr && s->path != SCLBM_PATH_TWO_PASS && fused_fits(s) &&
+    return s->ops->fused != nullptr && s->path != SCLBM_PATH_TWO_PASS && fused_fits(s) && s->sym_weights &&
            (!s->walls || s->ops->fused_walls != nullptr) && !s->simple_mode &&
            (!s->noise_kind || (s->ops->fused_noise != nullptr && !s->noise_indep && s->noise_sparse &&
                                (int64_t)s->noise_streams * s->V < ((int64_t)1 << 31)));
@@ -878,6 +898,7 @@ int sclbm_create(const sclbm_params *p, sclbm_sim **out) {
     }
     s->w.assign(p->w, p->w + p->q);
     s->we.assign(p->we, p->we + p->qe);
+    s->sym_weights = weights_symmetric(p);
     s->xi.assign(p->xi, p->xi + p->q * p->dim);
     s->e.assign(p->e, p->e + p->qe * p->dim);
     {
@@ -1105,9 +1126,11 @@ int sclbm_profile_step(sclbm_sim *s, int64_t nsteps, double *ms, int nms) {
 int sclbm_set_tuning(sclbm_sim *s, int path, int chunk) {
     if (!s) return fail(SCLBM_ERR_ARG, "null handle");
     if (path < SCLBM_PATH_AUTO || path > SCLBM_PATH_FUSED_PAIRS) return fail(SCLBM_ERR_ARG, "path %d", path);
-    const bool one_pass = path == SCLBM_PATH_FUSED || path == SCLBM_PATH_FUSED_PAIRS;
+    const bool one_pass = path >= SCLBM_PATH_FUSED;
     if (one_pass && !s->ops->fused)
         return fail(SCLBM_ERR_UNSUPPORTED, "single-pass kernel is built for FP32-shifted storage only");
+    if (one_pass && !s->sym_weights)
+        return fail(SCLBM_ERR_UNSUPPORTED, "single-pass kernel needs equal weights on opposite directions");
     if (one_pass && !fused_fits(s))
         return fail(SCLBM_ERR_UNSUPPORTED, "single-pass kernel needs q*volume < 2^31");
     DevGuard dg(s->device);
@@ -1652,6 +1675,8 @@ int sclbm_batch_create(const sclbm_params *p, int n, const int *sizes, const dou
         if (p->xi[i] != cx[i]) return fail(SCLBM_ERR_UNSUPPORTED, "lattice velocities differ");
     const int order = stencil_order(p->dim, p->e, p->qe);
     if (!order) return fail(SCLBM_ERR_UNSUPPORTED, "force stencil is not E4/E6/E8");
+    if (!weights_symmetric(p))
+        return fail(SCLBM_ERR_UNSUPPORTED, "batches need equal weights on opposite directions");
     if (p->collision != SCLBM_COLL_BGK || !(p->tau > 0))
         return fail(SCLBM_ERR_UNSUPPORTED, "batches run BGK with tau > 0");
     int ndev = 0;
