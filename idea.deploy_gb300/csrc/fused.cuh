@@ -420,11 +420,12 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
     }
 }
 
-// Three CTAs per SM for BGK (80 registers, no spills; 5% faster than two at
-// 256^3 D3Q19 E6, measured in one run), two for the dense MRT operator and
-// for the fluctuating step.
+// Resident CTAs per SM: BGK with paired halo loads four (64 registers, no
+// spills), BGK with one halo cell per load three (80 registers, no spills; 5%
+// faster than two at 256^3 D3Q19 E6, measured in one run), the dense MRT
+// operator two.
 template <class L, class S, bool MRT, bool PAIRS = false>
-__global__ void __launch_bounds__(FusedShape<L, S>::NT, MRT ? 2 : 3)
+__global__ void __launch_bounds__(FusedShape<L, S>::NT, MRT ? 2 : (PAIRS ? 4 : 3))
     k_fused(const float *__restrict__ pop, float *__restrict__ pop_out, const __grid_constant__ StepParams<L, S, float> p,
             const FusedGeom fg) {
     using SH = FusedShape<L, S>;

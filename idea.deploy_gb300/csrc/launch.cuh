@@ -57,7 +57,7 @@ struct KernelOps {
     cudaError_t (*fused)(const void *pop, void *pop_out, const void *step_params, const FusedGeom &fg, int grid,
                          cudaStream_t st);
     int fused_tx, fused_ty, fused_r;
-    int (*fused_occupancy)();
+    int (*fused_occupancy)(int pairs);  // of the paired-load instance when pairs != 0
     // batches of lattices (FP32 only, else null)
     cudaError_t (*batch_step)(const void *pop, void *pop_out, const void *sp, const BatchInst *inst, const int4 *items,
                               int n_items, int Vtot, int *counter, int parity, int grid, cudaStream_t st);
@@ -223,17 +223,18 @@ struct Ops {
             }
         }
     }
-    static int fused_occupancy() {
+    static int fused_occupancy(int pairs) {
         if constexpr (std::is_same<Real, float>::value) {
             using SH = FusedShape<L, S>;
             allow_smem();
             int b = 0;
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fused<L, S, MRT>, SH::NT, SH::SMEM);
             if constexpr (L::D == 3 && S::R % 2 == 0) {
-                int bp = 0;
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bp, k_fused<L, S, MRT, true>, SH::NT, SH::SMEM);
-                if (bp > 0 && bp < b) b = bp;
+                if (pairs) {
+                    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fused<L, S, MRT, true>, SH::NT, SH::SMEM);
+                    return b > 0 ? b : 1;
+                }
             }
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fused<L, S, MRT>, SH::NT, SH::SMEM);
             return b > 0 ? b : 1;
         }
         return 0;

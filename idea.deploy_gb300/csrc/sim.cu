@@ -464,9 +464,13 @@ void plan_fused(sclbm_sim *s) {
     g.tiles_x = (s->L[0] + o->fused_tx - 1) / o->fused_tx;
     g.tiles_y = s->D == 3 ? (s->L[1] + o->fused_ty - 1) / o->fused_ty : 1;
     const int Lm = s->D == 3 ? s->L[2] : s->L[1];
+    // paired halo loads where they apply (the automatic choice: 12-14% faster
+    // than one cell per load at 256^3 D3Q19 E6/E8, bit-identical results)
+    g.pairs = (s->path == SCLBM_PATH_FUSED_PAIRS || s->path == SCLBM_PATH_AUTO) && s->D == 3 && s->L[0] % 2 == 0 &&
+              o->fused_r % 2 == 0;
     const int resident = s->sms * (s->noise_kind ? o->fused_noise_occupancy()
                                    : s->walls    ? o->fused_walls_occupancy()
-                                                 : o->fused_occupancy());
+                                                 : o->fused_occupancy(g.pairs));
     const int base = g.tiles_x * g.tiles_y;
     int best_c = 1;
     double best = -1;
@@ -482,10 +486,6 @@ void plan_fused(sclbm_sim *s) {
             best_c = c;
         }
     }
-    // paired halo loads where they apply (the automatic choice: 12-14% faster
-    // than one cell per load at 256^3 D3Q19 E6/E8, bit-identical results)
-    g.pairs = (s->path == SCLBM_PATH_FUSED_PAIRS || s->path == SCLBM_PATH_AUTO) && s->D == 3 && s->L[0] % 2 == 0 &&
-              o->fused_r % 2 == 0;
     g.chunk = s->chunk_override > 0 ? std::min(s->chunk_override, Lm) : (Lm + best_c - 1) / best_c;
     g.chunks = (Lm + g.chunk - 1) / g.chunk;
     g.items = base * g.chunks;
@@ -1599,7 +1599,7 @@ void batch_items(const sclbm_batch *b, int chunk, std::vector<int4> &items) {
 }
 
 int batch_plan(sclbm_batch *b) {
-    const int resident = b->sms * b->ops->fused_occupancy();
+    const int resident = b->sms * b->ops->fused_occupancy(0);
     int chunk = BATCH_CHUNK;
     std::vector<int4> items;
     batch_items(b, chunk, items);
