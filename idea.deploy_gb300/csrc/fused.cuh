@@ -466,7 +466,7 @@ __global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
     }
 }
 
-template <class L, class S, class ST>
+template <class L, class S, class ST, bool PAIRS = false>
 __global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
     k_fused_noise(const float *__restrict__ pop, float *__restrict__ pop_out,
                   const __grid_constant__ StepParams<L, S, float> p, const FusedGeom fg, ST *__restrict__ seeds,
@@ -481,8 +481,9 @@ __global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
         const int iy = D == 3 ? rest % fg.tiles_y : 0;
         const int ic = D == 3 ? rest / fg.tiles_y : rest;
         const int m0 = ic * fg.chunk;
-        fused_tile<L, S, false, ST>(pop, pop_out, (int)fg.V, fg.L[0], fg.L[1], fg.L[2], ix * SH::TX, iy * SH::TY,
-                                    m0, min(m0 + fg.chunk, Lm), p.neg_g, p.rho0, p, smem, seeds, &z);
+        fused_tile<L, S, false, ST, false, PAIRS>(pop, pop_out, (int)fg.V, fg.L[0], fg.L[1], fg.L[2], ix * SH::TX,
+                                                  iy * SH::TY, m0, min(m0 + fg.chunk, Lm), p.neg_g, p.rho0, p, smem,
+                                                  seeds, &z);
     }
 }
 

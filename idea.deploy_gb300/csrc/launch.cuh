@@ -334,6 +334,19 @@ struct Ops {
             using SH = FusedShape<L, S>;
             allow_smem_noise();
             const NP &z = *static_cast<const NP *>(np);
+            if constexpr (L::D == 3 && S::R % 2 == 0) {
+                if (fg.pairs) {
+                    if (z.kind == CRNG_MMIX)
+                        k_fused_noise<L, S, unsigned long long, true><<<grid, SH::NT, SH::NSMEM, st>>>(
+                            (const float *)pop, (float *)pop_out, *static_cast<const SP *>(sp), fg,
+                            (unsigned long long *)seeds, z);
+                    else
+                        k_fused_noise<L, S, unsigned int, true><<<grid, SH::NT, SH::NSMEM, st>>>(
+                            (const float *)pop, (float *)pop_out, *static_cast<const SP *>(sp), fg,
+                            (unsigned int *)seeds, z);
+                    return cudaGetLastError();
+                }
+            }
             if (z.kind == CRNG_MMIX)
                 k_fused_noise<L, S, unsigned long long><<<grid, SH::NT, SH::NSMEM, st>>>(
                     (const float *)pop, (float *)pop_out, *static_cast<const SP *>(sp), fg, (unsigned long long *)seeds,
@@ -355,6 +368,12 @@ struct Ops {
                                      FusedShape<L, S>::NSMEM);
                 cudaFuncSetAttribute(k_fused_noise<L, S, unsigned long long>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, FusedShape<L, S>::NSMEM);
+                if constexpr (L::D == 3 && S::R % 2 == 0) {
+                    cudaFuncSetAttribute(k_fused_noise<L, S, unsigned int, true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, FusedShape<L, S>::NSMEM);
+                    cudaFuncSetAttribute(k_fused_noise<L, S, unsigned long long, true>,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, FusedShape<L, S>::NSMEM);
+                }
                 if (dev >= 0 && dev < 64) done[dev] = true;
             }
         }

@@ -1146,9 +1146,9 @@ int sclbm_set_tuning(sclbm_sim *s, int path, int chunk) {
 int sclbm_get_tuning(const sclbm_sim *s, int *path, int *chunk, int *grid) {
     if (!s) return fail(SCLBM_ERR_ARG, "null handle");
     if (path)
-        *path = !fused_path(s)                               ? SCLBM_PATH_TWO_PASS
-                : s->fg.pairs && !s->walls && !s->noise_kind ? SCLBM_PATH_FUSED_PAIRS
-                                                             : SCLBM_PATH_FUSED;
+        *path = !fused_path(s)               ? SCLBM_PATH_TWO_PASS
+                : s->fg.pairs && !s->walls ? SCLBM_PATH_FUSED_PAIRS
+                                             : SCLBM_PATH_FUSED;
     if (chunk) *chunk = fused_path(s) ? s->fg.chunk : 0;
     if (grid) *grid = fused_path(s) ? s->fused_grid : s->fgrid;
     return SCLBM_OK;

@@ -230,3 +230,32 @@ def test_zero_generator_state_stays_finite():
     assert rel_err(got[~bad], want[~bad]) < 1e-12
     assert np.array_equal(s.get_seeds(_lib.SEEDS_CELL_MAJOR), ora.get_seeds())
     s.close()
+
+
+@pytest.mark.parametrize('st,kind,dims', [('D3E6', 'MINSTD', (40, 36, 32)), ('D3E6', 'MMIX', (66, 18, 20)),
+                                          ('D3E8', 'NUMREC', (32, 32, 24))])
+def test_fp32_single_pass_paired_halo_loads_bit_identical(st, kind, dims):
+    """The fluctuating single pass with paired halo loads gives the same
+    populations and generator states, bit for bit, as with one halo cell per
+    load (the sums run in the same order)."""
+    x, f = XIStencils['D3Q19'], FStencils[st]
+    from sclbm.profiles import droplet
+    n_init = droplet(dims, 8.0, 4.5625, 0.2086, 2.0, 5)
+    nr, ns = _lib.noise_counts(3, 19, False)
+    dt = np.uint64 if kind == 'MMIX' else np.uint32
+    seeds = np.random.default_rng(11).integers(1, 2 ** 31 - 2, ns * n_init.size, dtype=np.int64).astype(dt)
+    out = []
+    for path in (_lib.PATH_FUSED, _lib.PATH_FUSED_PAIRS):
+        s = _lib.Sim(3, dims, x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], -4.5, precision=_lib.FP32_SHIFTED,
+                     rho0=0.2086)
+        s.set_density(n_init)
+        s.set_velocity(np.zeros(3 * s.V))
+        s.init_populations()
+        s.set_tuning(path, 5)
+        s.set_fluctuations(kind, False, 1e-5, 1.0, seeds)
+        assert s.get_tuning()[0] == path and s.kernels_per_step() == 1
+        s.step(20)
+        out.append((s.get_populations(), s.get_seeds()))
+        s.close()
+    assert np.array_equal(out[0][1], out[1][1])
+    assert np.array_equal(out[0][0], out[1][0])
