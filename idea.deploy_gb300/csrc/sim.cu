@@ -1718,7 +1718,6 @@ int sclbm_batch_create(const sclbm_params *p, int n, const int *sizes, const dou
     b->steps.assign(n, 0);
     // lattices and work items (lattice-major so concurrent items are neighbours)
     int64_t base = 0;
-    const int TX = b->ops->fused_tx, TY = b->ops->fused_ty;
     for (int i = 0; i < n; i++) {
         const int *L = &b->sizes[(size_t)i * b->D];
         BatchInst I;

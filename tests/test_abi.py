@@ -66,6 +66,30 @@ def test_create_rejects_bad_tables_before_touching_the_device():
     assert e.value.status == _lib.ERR_ARG
 
 
+def test_batch_rejects_unequal_weights_on_opposite_vectors():
+    """The single-pass kernels pair every force-stencil vector with its
+    opposite (one psi difference per pair), so a stencil whose opposite
+    vectors carry different weights is refused before the device is touched."""
+    from sclbm.batch import Batch
+    x, f = XIStencils['D2Q9'], FStencils['D2E4']
+    ws = list(f['Ws'])
+    ws[0] = ws[0] * 1.5
+    bad = dict(f, Ws=ws)
+    with pytest.raises(_lib.SclbmError) as e:
+        Batch(x, bad, [(32, 32)], [-4.5], [1.0])
+    assert e.value.status == _lib.ERR_UNSUPPORTED
+    assert 'opposite' in str(e.value)
+    try:
+        import torch
+        if torch.cuda.is_available():
+            return
+    except ImportError:
+        pass
+    with pytest.raises(_lib.SclbmError) as e:
+        Batch(x, f, [(32, 32)], [-4.5], [1.0])   # symmetric: passes the check, no device
+    assert e.value.status in (_lib.ERR_NODEVICE, _lib.ERR_CUDA)
+
+
 @pytest.mark.parametrize('missing,msg', [
     ('f_stencil', "Missing 'f_stencil'"), ('tau', "Missing 'tau'"), ('SC_G', "Missing 'SC_G'"),
     ('psi_code', "Missing 'psi_code'"), ('lang', 'Param lang'), ('psi_sym', "parameter 'psi_sym'")])
