@@ -501,7 +501,9 @@ struct BatchInst {
     int active, pad;
 };
 
-template <class L, class S, bool MRT>
+// PAIRS: every lattice has an even Lx and an even first cell (base) and the
+// total volume is even, so the paired halo loads of fused_tile stay aligned
+template <class L, class S, bool MRT, bool PAIRS = false>
 __global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
     k_fused_batch(const float *__restrict__ pop, float *__restrict__ pop_out,
                   const __grid_constant__ StepParams<L, S, float> p, const BatchInst *__restrict__ inst,
@@ -519,8 +521,8 @@ __global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
         const int4 w = items[it];  // lattice, x0, y0, m0 | m1 << 16
         const BatchInst I = inst[w.x];
         if (!I.active) continue;
-        fused_tile<L, S, MRT>(pop + I.base, pop_out + I.base, Vtot, I.Lx, I.Ly, I.Lz, w.y, w.z, w.w & 0xffff,
-                              w.w >> 16, I.neg_g, I.rho0, p, smem);
+        fused_tile<L, S, MRT, void, false, PAIRS>(pop + I.base, pop_out + I.base, Vtot, I.Lx, I.Ly, I.Lz, w.y, w.z,
+                                                  w.w & 0xffff, w.w >> 16, I.neg_g, I.rho0, p, smem);
     }
 }
 

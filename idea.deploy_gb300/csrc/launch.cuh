@@ -60,7 +60,7 @@ struct KernelOps {
     int (*fused_occupancy)(int pairs);  // of the paired-load instance when pairs != 0
     // batches of lattices (FP32 only, else null)
     cudaError_t (*batch_step)(const void *pop, void *pop_out, const void *sp, const BatchInst *inst, const int4 *items,
-                              int n_items, int Vtot, int *counter, int parity, int grid, cudaStream_t st);
+                              int n_items, int Vtot, int *counter, int parity, int pairs, int grid, cudaStream_t st);
     cudaError_t (*batch_density)(const void *pop, void *dn, void *psi, const void *sp, const BatchInst *inst, int n_inst,
                                  int Vtot, int gx, cudaStream_t st);
     cudaError_t (*batch_moments)(const void *pop, const void *dn, const void *psi, void *u_old, const void *sp,
@@ -240,8 +240,8 @@ struct Ops {
         return 0;
     }
     static cudaError_t batch_step(const void *pop, void *pop_out, const void *sp, const BatchInst *inst,
-                                  const int4 *items, int n_items, int Vtot, int *counter, int parity, int grid,
-                                  cudaStream_t st) {
+                                  const int4 *items, int n_items, int Vtot, int *counter, int parity, int pairs,
+                                  int grid, cudaStream_t st) {
         if constexpr (std::is_same<Real, float>::value) {
             using SH = FusedShape<L, S>;
             static bool done[64] = {};
@@ -249,7 +249,18 @@ struct Ops {
             cudaGetDevice(&dev);
             if (dev < 0 || dev >= 64 || !done[dev]) {
                 cudaFuncSetAttribute(k_fused_batch<L, S, MRT>, cudaFuncAttributeMaxDynamicSharedMemorySize, SH::SMEM);
+                if constexpr (L::D == 3 && S::R % 2 == 0)
+                    cudaFuncSetAttribute(k_fused_batch<L, S, MRT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         SH::SMEM);
                 if (dev >= 0 && dev < 64) done[dev] = true;
+            }
+            if constexpr (L::D == 3 && S::R % 2 == 0) {
+                if (pairs) {
+                    k_fused_batch<L, S, MRT, true><<<grid, SH::NT, SH::SMEM, st>>>(
+                        (const float *)pop, (float *)pop_out, *static_cast<const SP *>(sp), inst, items, n_items, Vtot,
+                        counter, parity);
+                    return cudaGetLastError();
+                }
             }
             k_fused_batch<L, S, MRT><<<grid, SH::NT, SH::SMEM, st>>>((const float *)pop, (float *)pop_out,
                                                                      *static_cast<const SP *>(sp), inst, items,

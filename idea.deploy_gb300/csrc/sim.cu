@@ -1538,6 +1538,7 @@ struct sclbm_batch {
     double *probe_d = nullptr;  // [2n] centre / last-cell densities
     float *delta_d = nullptr;   // [n] rest-population corrections
     int gx = 1, grid = 1, chunk = 32;
+    int pairs = 0;          // 3D, even radius, every Lx and first cell even: paired halo loads
     std::vector<int> home;  // buffer holding a retired lattice's state (-1 while active)
     std::vector<int64_t> steps;
     bool pop_set = false;
@@ -1621,7 +1622,8 @@ int batch_plan(sclbm_batch *b) {
 
 int batch_launch_step(sclbm_batch *b) {
     cudaError_t e = b->ops->batch_step(b->pop[b->cur], b->pop[b->cur ^ 1], b->sp.data(), b->inst_d, b->items_d,
-                                       (int)b->items.size(), (int)b->Vtot, b->counter, b->cur, b->grid, b->st);
+                                       (int)b->items.size(), (int)b->Vtot, b->counter, b->cur, b->pairs, b->grid,
+                                       b->st);
     if (e != cudaSuccess) return fail(SCLBM_ERR_CUDA, "batch step: %s", cudaGetErrorString(e));
     b->cur ^= 1;
     return SCLBM_OK;
@@ -1732,6 +1734,9 @@ int sclbm_batch_create(const sclbm_params *p, int n, const int *sizes, const dou
         b->inst.push_back(I);
         base += lattice_cells(b, i);
     }
+    // paired halo loads when every lattice keeps them aligned
+    b->pairs = b->D == 3 && b->ops && b->ops->fused_r % 2 == 0 && Vtot % 2 == 0;
+    for (const BatchInst &I : b->inst) b->pairs = b->pairs && I.Lx % 2 == 0 && I.base % 2 == 0;
     // step parameters (BGK, FP32); G and rho0 come from the lattice table
     CollisionSpec cs;
     cs.dim = b->D;

@@ -13,6 +13,8 @@ pytestmark = pytest.mark.gpu
 CASES = {
     '2d': ('D2Q9', 'D2E8', [(64, 64), (96, 96), (32, 32)], [-4.5, -5.0, -4.8], [0.8, 2.0, 1.0]),
     '3d': ('D3Q19', 'D3E6', [(32, 32, 32), (48, 40, 36)], [-4.5, -4.7], [1.0, 2.4]),
+    # an odd Lx: the whole batch keeps one halo cell per load
+    '3d_odd': ('D3Q19', 'D3E6', [(33, 20, 16), (32, 32, 24)], [-4.5, -4.7], [1.0, 2.4]),
 }
 
 
@@ -26,7 +28,7 @@ def densities(dims_list):
     return [droplet(d, min(d) / 4.0, 4.6, 0.2, 2.0, 30 + i) for i, d in enumerate(dims_list)]
 
 
-@pytest.mark.parametrize('case', ['2d', '3d'])
+@pytest.mark.parametrize('case', ['2d', '3d', '3d_odd'])
 def test_batch_matches_single_lattices(case):
     lat, st, dims, G, rho0 = CASES[case]
     n0 = densities(dims)
