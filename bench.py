@@ -36,6 +36,9 @@ R, RHO_L, RHO_G, WIDTH, SEED, G = 40.0, 2.2, 0.15, 2.0, 1234, -5.0
 Q = 19
 WORKLOAD = ('D3Q19 E6 MRT (all rates 1.0) + Guo, psi=exp(-1/rho), G=-5.0, 256^3 periodic, '
             'droplet R=40 tanh width 2, rho_l=2.2 rho_g=0.15, 1e-4 seeded noise')
+# the stable twin of the headline (G=-5 diverges in the reference as well):
+# G=-4.5 with the 3D E6 flat-interface densities
+G_STABLE, RHO_L_STABLE, RHO_G_STABLE = -4.5, 4.636, 0.147
 
 
 def dist_env():
@@ -235,14 +238,121 @@ def peaks():
         return None
 
 
-def make_sim(precision, device, literals='exact'):
+def make_sim(precision, device, literals='exact', box=None, g=None, rho0=None):
     from sclbm import _lib, XIStencils, FStencils
     x, f = XIStencils['D3Q19'], FStencils['D3E6']
     S = np.eye(Q)
-    return _lib.Sim(3, BOX, x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], G, collision=_lib.COLL_MRT, mrt_s=S,
+    return _lib.Sim(3, box or BOX, x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], G if g is None else g,
+                    collision=_lib.COLL_MRT, mrt_s=S,
                     precision=_lib.FP32_SHIFTED if precision == 'fp32' else _lib.FP64,
-                    rho0=0.5 * (RHO_L + RHO_G), device=device,
+                    rho0=0.5 * (RHO_L + RHO_G) if rho0 is None else rho0, device=device,
                     literals=_lib.LIT_EXACT if literals == 'exact' else _lib.LIT_ROUND15)
+
+
+def stable_twin(dev, steps, ms_headline):
+    """The headline's kernel on the same box at the stable coupling G=-4.5:
+    the step does the same work whatever the data (no branch depends on it),
+    so its time should equal the headline's, which diverges to NaN."""
+    from sclbm.profiles import droplet
+    n0 = droplet(BOX, R, RHO_L_STABLE, RHO_G_STABLE, WIDTH, SEED)
+    s = make_sim('fp32', dev, g=G_STABLE, rho0=0.5 * (RHO_L_STABLE + RHO_G_STABLE))
+    s.set_density(n0)
+    s.set_velocity(np.zeros(3 * n0.size))
+    s.init_populations()
+    s.step(5)
+    ms = s.step_timed(steps)
+    finite, nmax = s.density_finite()
+    s.close()
+    return {'G': G_STABLE, 'rho_l': RHO_L_STABLE, 'rho_g': RHO_G_STABLE, 'steps': steps,
+            'ms_per_step': round(ms / steps, 5), 'value': round(n0.size * steps / (ms / 1e3) / 1e6, 1),
+            'unit': 'MLUPS', 'ratio_to_headline_step': round(ms / steps / ms_headline, 4),
+            'finite_density_at_end': finite, 'max_density_at_end': nmax}
+
+
+def precision_table(dev, L=128, steps=5000):
+    """FP32-shifted storage against the plain FP64 path on the 3D headline's
+    shape at the stable coupling: D3Q19 E6, MRT rates 1.0, droplet R = L*40/256,
+    G=-4.5, `steps` steps; errors of the density and velocity fields, of the
+    mass, of the Laplace pressure (PBulk of the centre and corner densities),
+    and of the spurious-current magnitude max|u|.  Two FP32 shifts: the gas
+    density (the library's choice for droplets) and the mean of the two
+    densities (the headline's)."""
+    from sclbm.profiles import droplet
+    from sclbm.sweep import laplace_dp
+    box = (L, L, L)
+    n0 = droplet(box, L * 40.0 / 256, RHO_L_STABLE, RHO_G_STABLE, WIDTH, SEED)
+    V = n0.size
+    c = L // 2
+    probe = [c + L * c + L * L * c, V - 1]
+
+    def run(prec, rho0=None):
+        s = make_sim(prec, dev, box=box, g=G_STABLE, rho0=rho0)
+        s.set_density(n0)
+        s.set_velocity(np.zeros(3 * V))
+        s.init_populations()
+        m0, _ = s.reductions()
+        t0 = time.perf_counter()
+        s.step(steps)
+        wall = time.perf_counter() - t0
+        s.compute_moments()
+        n, u = s.get_density(), s.get_velocity().reshape(3, -1)
+        m1, _ = s.reductions()
+        ni, no = s.density_at(probe)
+        s.close()
+        return dict(n=n, u=u, mass_drift=(m1 - m0) / m0, dp=laplace_dp(ni, no, G_STABLE)[0], n_in=ni, n_out=no,
+                    umax=float(np.sqrt((u ** 2).sum(0)).max()), wall=wall)
+
+    ref = run('fp64')
+    out = {'box': list(box), 'steps': steps, 'G': G_STABLE, 'R': L * 40.0 / 256,
+           'reference': 'plain FP64 GPU path (exact coefficients; within 1e-10 of the reference on the 2D twin)',
+           'fp64': {'mass_drift': ref['mass_drift'], 'dp': ref['dp'], 'rho_in': ref['n_in'], 'rho_out': ref['n_out'],
+                    'max_u': ref['umax'], 'wall_s': round(ref['wall'], 3)}}
+    umag = np.sqrt((ref['u'] ** 2).sum(0))
+    for key, rho0 in (('fp32_shift_gas', RHO_G_STABLE), ('fp32_shift_mid', 0.5 * (RHO_L_STABLE + RHO_G_STABLE))):
+        r = run('fp32', rho0)
+        dn = np.abs(r['n'] - ref['n'])
+        du = np.sqrt(((r['u'] - ref['u']) ** 2).sum(0))
+        out[key] = {'rho0': rho0,
+                    'n_rel_err_max': float(dn.max() / np.abs(ref['n']).max()),
+                    'n_rel_err_median': float(np.median(dn / np.abs(ref['n']))),
+                    'u_err_max_over_max_u': float(du.max() / umag.max()),
+                    'u_err_median_over_max_u': float(np.median(du) / umag.max()),
+                    'mass_drift': r['mass_drift'],
+                    'dp_rel_err': float(abs(r['dp'] - ref['dp']) / abs(ref['dp'])),
+                    'rho_in_rel_err': float(abs(r['n_in'] - ref['n_in']) / ref['n_in']),
+                    'rho_out_rel_err': float(abs(r['n_out'] - ref['n_out']) / ref['n_out']),
+                    'max_u_rel_err': float(abs(r['umax'] - ref['umax']) / ref['umax']),
+                    'wall_s': round(r['wall'], 3)}
+    return out
+
+
+def sweep_leg(dev, max_steps=100000, coex_steps=100000):
+    """Cfg 3's ragged sweep (64 D2Q9 E8 droplets, R = 8..71) bounded for the
+    default run: the batched FP32 path and the plain FP64 path droplet by
+    droplet, both stopped by the same criterion (the Laplace pressure calm to
+    2e-5 over 4 checks of 500 steps); wall time to converge, speed-up, and the
+    Laplace-pressure error of the batch against the FP64 runs."""
+    from sclbm import sweep
+    r = sweep.run_sweep(n=64, max_steps=max_steps, coex_steps=coex_steps, plain=True, device=dev,
+                        plain_stop_at_dp=True)
+    b = r['batch']
+    plain = r['plain']
+    both = [j for j, p in enumerate(plain)
+            if p is not None and p['status'] == 'converged' and b['status'][j] == 'converged']
+    errs = np.array([abs(b['dp'][j] - plain[j]['dp']) / abs(plain[j]['dp']) for j in both])
+    return {'droplets': 64, 'criterion': 'both arms: Laplace pressure calm to 2e-5 over 4 checks (500 steps apart)',
+            'coexistence_wall_s': round(r['coexistence_wall_s'], 2),
+            'batch_fp32': {'wall_s': round(b['wall_s'], 3),
+                           'status': {str(k): int((b['status'] == k).sum()) for k in set(b['status'])},
+                           'steps_max': int(np.max(b['steps']))},
+            'plain_fp64': {'wall_s': round(r['plain_wall_s'], 3),
+                           'status': {k: sum(1 for p in plain if p is not None and p['status'] == k)
+                                      for k in ('converged', 'max_steps', 'diverged')}},
+            'speedup_wall': round(r['plain_wall_s'] / b['wall_s'], 2),
+            'dp_rel_err_vs_fp64': {'median': float(np.median(errs)) if errs.size else None,
+                                   'max': float(errs.max()) if errs.size else None,
+                                   'within_1e-5': int((errs <= 1e-5).sum()), 'n': int(errs.size)},
+            'unstable': len(r['unstable'])}
 
 
 def profiled_traffic():
@@ -256,7 +366,7 @@ def profiled_traffic():
         return None, None
 
 
-def e2e_measure(precision, device, iters=3, lbm_steps=200):
+def e2e_measure(precision, device, iters=3, lbm_steps=200, g=None, rho_l=None, rho_g=None):
     """Through the public API with host buffers: H2D of the initial density and
     velocity from pinned host memory, InitPopulations, MainLoop over lbm_steps,
     GetDensityField (D2H).  The library reads and writes the FP64 host arrays
@@ -275,13 +385,16 @@ def e2e_measure(precision, device, iters=3, lbm_steps=200):
         out[:] = a.ravel()
         return out, t
 
-    n0, keep_n = pinned(droplet(BOX, R, RHO_L, RHO_G, WIDTH, SEED))
+    g = G if g is None else g
+    rho_l = RHO_L if rho_l is None else rho_l
+    rho_g = RHO_G if rho_g is None else rho_g
+    n0, keep_n = pinned(droplet(BOX, R, rho_l, rho_g, WIDTH, SEED))
     u0, keep_u = pinned(np.zeros(3 * n0.size))
     res, keep_r = pinned(np.zeros(n0.size))   # the result buffer, pinned as well
     sc = ShanChenMultiPhase(lang=CUDA_T, dim_sizes=BOX, xi_stencil=XIStencils['D3Q19'],
-                            f_stencil=FStencils['D3E6'], psi_code='exp(-1./ln_0)', psi_sym=None, SC_G=G,
+                            f_stencil=FStencils['D3E6'], psi_code='exp(-1./ln_0)', psi_sym=None, SC_G=g,
                             tau=1.0, precision='fp32_shifted' if precision == 'fp32' else 'fp64',
-                            rho0=0.5 * (RHO_L + RHO_G), device=device)
+                            rho0=0.5 * (rho_l + rho_g), device=device)
     pageable = sc._sim.set_transfer(_lib.TRANSFER_AUTO)
     syms = [sp.Symbol('w%d' % i) for i in range(Q)]
     mrt = dict(relaxation_matrix=sp.Matrix.diag(syms), omega_syms_vals=[(s, 1.0) for s in syms])
@@ -306,7 +419,7 @@ def e2e_measure(precision, device, iters=3, lbm_steps=200):
             'step': 'one job: H2D rho and u (FP64 pinned host arrays, read by a kernel over the link), '
                     'InitPopulations, MainLoopMRT over %d lattice steps, GetDensityField into a pinned FP64 '
                     'result array (written by a kernel)' % lbm_steps,
-            'pageable_host_access': pageable,
+            'pageable_host_access': pageable, 'G': g,
             'seconds_per_job': round(dt, 4), 'finite_density': bool(np.isfinite(n).all())}
 
 
@@ -425,6 +538,13 @@ def run_ours(a, dist):
                               'alg_bytes_per_cell': (2 * Q * 4 + 2 * nr * 4),
                               'achieved_GBs': round(ach_f, 1), 'frac': round(ach_f / hbm, 4)}
         out['e2e'] = e2e_measure('fp32', dev)
+        # the same job at the stable coupling: a finite result, the same cost
+        out['e2e_stable'] = e2e_measure('fp32', dev, g=G_STABLE, rho_l=RHO_L_STABLE, rho_g=RHO_G_STABLE)
+        out['stable_twin'] = stable_twin(dev, max(20, min(a.steps, 400)), ms / a.steps)
+        if not a.no_precision:
+            out['fp32_vs_fp64'] = precision_table(dev, L=a.precision_box, steps=a.precision_steps)
+        if not a.no_sweep:
+            out['sweep'] = sweep_leg(dev)
         if not a.no_cpu:
             out['cpu_baseline'] = cpu_measure(a.cpu_seconds)
     return out
@@ -629,6 +749,10 @@ def main():
     # profiling case: a smaller cubic box and only the main (FP32 single-pass) leg
     ap.add_argument('--box', type=int, default=0, help='cube side for a profiling run (default 256)')
     ap.add_argument('--main-only', action='store_true', help='skip the secondary legs')
+    ap.add_argument('--no-precision', action='store_true', help='skip the FP32-vs-FP64 error table')
+    ap.add_argument('--precision-box', type=int, default=128)
+    ap.add_argument('--precision-steps', type=int, default=5000)
+    ap.add_argument('--no-sweep', action='store_true', help='skip the bounded droplet-sweep leg')
     a = ap.parse_args()
     if a.box:
         global BOX

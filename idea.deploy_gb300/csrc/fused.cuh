@@ -19,10 +19,21 @@
 // 2R+1 per-plane slot bases.
 #pragma once
 
+#include <cuda.h>  // CUtensorMap (the tensor maps are encoded on the host)
+
 #include "kernels.cuh"
 #include "noise.cuh"
 
 namespace sclbm {
+
+// Staging of the 3D single pass (bit flags; 0 = every load straight into registers):
+//   STG_HALO_ASYNC  the halo pairs of plane m+R+1 are copied into this thread's
+//                   own shared-memory slots with cp.async while plane m collides
+//                   (each thread reads back only what it copied: no barrier)
+//   STG_OWN_TMA     the tile's own populations of plane m+1 come in by one TMA
+//                   box (x, y, plane, q) = (TX, TY, 1, Q) per plane, double
+//                   buffered, completed on an mbarrier, while plane m collides
+enum : int { STG_HALO_ASYNC = 1, STG_OWN_TMA = 2 };
 
 template <class L, class S>
 struct FusedShape {
@@ -45,7 +56,68 @@ struct FusedShape {
     static constexpr int NSMEM = SMEM + (L::Q - D - 1) * NT * 4;
     // walls: plus a ring of the halo planes' wall flags (bytes)
     static constexpr int WSMEM = SMEM + (RING * HC + 3) / 4 * 4;
+    // staged variants (3D): halo-pair slots [Q][HSTR] float2, then two own
+    // buffers [Q][TY][TX] float (128-byte aligned: TMA destinations) and their
+    // two mbarriers
+    static constexpr int NPAIR = (HX / 2) * HY;
+    static constexpr int HSTR = (NPAIR + 31) / 32 * 32;
+    static constexpr int RING_BYTES = RING * HC * 4;
+    static constexpr int HALO_BYTES = L::Q * HSTR * 8;
+    static constexpr int OWN_BOX_BYTES = L::Q * NT * 4;
+    static constexpr int own_offset(int stg) {
+        return ((RING_BYTES + ((stg & STG_HALO_ASYNC) ? HALO_BYTES : 0)) + 127) / 128 * 128;
+    }
+    static constexpr int stg_smem(int stg) {
+        return (stg & STG_OWN_TMA) ? own_offset(stg) + 2 * OWN_BOX_BYTES + 16
+                                   : RING_BYTES + ((stg & STG_HALO_ASYNC) ? HALO_BYTES : 0);
+    }
 };
+
+// ---- PTX helpers of the staged variants ------------------------------------
+__device__ __forceinline__ unsigned smem_u32(const void *p) { return (unsigned)__cvta_generic_to_shared(p); }
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(smem_u32(smem)), "l"(gmem) : "memory");
+}
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// box (c0, c1, c2, c3) of a 4D tensor map into shared memory, completing on bar
+__device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, uint64_t *bar, int c0, int c1, int c2,
+                                            int c3) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4, "
+        "%5}], [%6];\n" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(c0), "r"(c1), "r"(c2), "r"(c3), "r"(smem_u32(bar))
+        : "memory");
+}
+// Bounded wait on an mbarrier phase: a TMA that never completes (it cannot,
+// unless the tensor map or the byte count is wrong) must not hang the GPU.
+// After MBAR_POLLS unsuccessful polls the wait gives up, records the failure in
+// *err (read by the host after the launch) and the kernel runs on with the
+// buffer as it is (no thread leaves the block's barriers); later waits of the
+// launch then return at once.
+constexpr int MBAR_POLLS = 1 << 20;
+__device__ __forceinline__ void mbar_wait_bounded(uint64_t *bar, unsigned parity, int *err, bool &dead) {
+    if (dead) return;
+    for (int i = 0; i < MBAR_POLLS; i++)
+        if (mbar_try_wait(bar, parity)) return;
+    dead = true;
+    if (err) atomicOr(err, 1);
+}
 
 __device__ __forceinline__ void cp_async4(float *smem, const float *gmem) {
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
@@ -63,6 +135,8 @@ struct FusedGeom {
     int tiles_x, tiles_y, chunks, chunk;  // work decomposition
     int items;
     int pairs;  // 3D, even Lx and even halo radius: halo populations loaded two cells per load
+    int stg;    // STG_* flags of the staged 3D variants (0: none)
+    int *err;   // device flag set by a staged variant whose bounded wait gave up
 };
 
 // FP32 pseudopotential with the fast hardware exp2/reciprocal (relative error
@@ -147,15 +221,24 @@ SCLBM_HD constexpr int opposite_e(int a) {
 // and address instructions of the scalar form (two cells per thread, the
 // second re-read by threads that have none).  The sums run in the same order,
 // so the results are bit-identical to the scalar form.
-template <class L, class S, bool MRT, class ST = void, bool WALLS = false, bool PAIRS = false>
+// STG (3D, PAIRS, no walls or noise): STG_* staging flags.  With STG_OWN_TMA
+// the caller passes the input's tensor map, the two mbarriers, the running
+// issue / wait counts of own-population boxes (k_issue-th box: buffer k & 1,
+// phase (k >> 1) & 1, the same on every thread) and the error flag.
+template <class L, class S, bool MRT, class ST = void, bool WALLS = false, bool PAIRS = false, int STG = 0>
 __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float *__restrict__ pop_out, const int V,
                                            const int Lx, const int Ly, const int Lz, const int x0, const int y0,
                                            const int m0, const int m1, const float neg_g, const float rho0,
                                            const StepParams<L, S, float> &p, float *smem,
                                            ST *seeds = nullptr, const NoiseParams<L, float> *z = nullptr,
                                            const unsigned char *__restrict__ walls = nullptr,
-                                           const float *__restrict__ psi_w = nullptr) {
+                                           const float *__restrict__ psi_w = nullptr,
+                                           const CUtensorMap *tmap = nullptr, uint64_t *bars = nullptr,
+                                           unsigned *k_issue = nullptr, unsigned *k_wait = nullptr,
+                                           int *err = nullptr, bool *dead = nullptr) {
     constexpr bool NOISE = !std::is_void<ST>::value;
+    static_assert(STG == 0 || (PAIRS && !NOISE && !WALLS && L::D == 3), "staged variants: 3D paired halo loads");
+    constexpr bool HALO_ASYNC = (STG & STG_HALO_ASYNC) != 0, OWN_TMA = (STG & STG_OWN_TMA) != 0;
     using SeedT = typename std::conditional<NOISE, ST, int>::type;
     using SH = FusedShape<L, S>;
     constexpr int D = L::D, Q = L::Q, R = SH::R, HX = SH::HX, HC = SH::HC, NT = SH::NT, RING = SH::RING;
@@ -193,7 +276,7 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
         X3[o + 1] = wrapc(x + o, Lx);
         Y3[o + 1] = D == 3 ? Lx * wrapc(y + o, Ly) : 0;
     }
-    const int own = X3[1] + Y3[1];
+    const int own_cell = X3[1] + Y3[1];
 
     // n and psi of plane m straight from global memory; every load is issued
     // before the first sum (threads without a second halo cell re-read their
@@ -285,23 +368,73 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
         }
     };
 
+    // STG_HALO_ASYNC: this thread's halo pair of plane m copied into its own
+    // slots hst[q*HSTR + tid] (issued one plane ahead), reduced from there
+    float2 *hst = reinterpret_cast<float2 *>(smem + RING * HC);
+    auto halo_issue = [&](int m) {
+        if constexpr (HALO_ASYNC) {
+            if (tid < NPAIR) {
+                const float2 *src = reinterpret_cast<const float2 *>(pop + (wrapm(m, Lm) * PL + hoffp));
+                const int V2 = V >> 1;
+#pragma unroll
+                for (int q = 0; q < Q; q++) cp_async8(hst + q * SH::HSTR + tid, src + q * V2);
+            }
+            cp_async_commit();
+        }
+    };
+    auto halo_reduce = [&](int m) {
+        if constexpr (HALO_ASYNC) {
+            cp_async_wait<0>();
+            if (tid < NPAIR) {
+                float2 w[Q];
+#pragma unroll
+                for (int q = 0; q < Q; q++) w[q] = hst[q * SH::HSTR + tid];
+                float sx = w[lex_q<Q>(0)].x, sy = w[lex_q<Q>(0)].y;
+#pragma unroll
+                for (int i = 1; i < Q; i++) {
+                    sx += w[lex_q<Q>(i)].x;
+                    sy += w[lex_q<Q>(i)].y;
+                }
+                // the store needs every value read back, so the next cp.async
+                // into these slots (issued after it) cannot overtake the reads
+                reinterpret_cast<float2 *>(ring + wrapm(m, RING) * HC)[tid] =
+                    make_float2(psi_fast(p.psi_kind, rho0 + sx), psi_fast(p.psi_kind, rho0 + sy));
+            }
+        }
+    };
+    // STG_OWN_TMA: the tile's populations of plane m, box (x0, y0, plane, 0),
+    // into own buffer b (thread 0 issues)
+    float *own = reinterpret_cast<float *>(reinterpret_cast<char *>(smem) + SH::own_offset(STG));
+    auto own_issue = [&](int m) {
+        if constexpr (OWN_TMA) {
+            const int b = *k_issue & 1;
+            if (tid == 0) {
+                mbar_expect_tx(&bars[b], SH::OWN_BOX_BYTES);
+                tma_load_4d(own + b * (SH::OWN_BOX_BYTES / 4), tmap, &bars[b], x0, y0, wrapm(m, Lm), 0);
+            }
+            (*k_issue)++;
+        }
+    };
+
     // 2D: the halo of plane m+R+1 is prefetched with cp.async during plane m;
     // 3D: the halo (1.7x the tile) is reduced straight from L2 and the
     // thread's own populations of plane m are loaded first, so both sets of
     // loads are in flight together
     constexpr bool STAGED = D == 2;
-    __syncthreads();  // the previous item's readers are done with the ring
+    __syncthreads();  // the previous item's readers are done with the ring (and the own buffers)
+    own_issue(m0);
     for (int m = m0 - R; m < m0 + R; m++) psi_plane(m);
     if (STAGED) stage_issue(m0 + R);
+    halo_issue(m0 + R);
     for (int m = m0; m < m1; m++) {
         int Z3[3];
 #pragma unroll
         for (int o = -1; o <= 1; o++) Z3[o + 1] = D == 3 ? wrapc(m + o, Lm) * PL : wrapc(m + o, Lm) * Lx;
-        const int g = own + Z3[1];
+        const int g = own_cell + Z3[1];
         float f[Q];
         constexpr int NR = NoiseParams<L, float>::NR;
         SeedT st[NOISE ? NR : 1];
-        if (in_tile) {
+        if (in_tile && !OWN_TMA) {
 #pragma unroll
             for (int q = 0; q < Q; q++) f[q] = __ldg(pop + (g + q * V));
             // generator states with the populations: their loads overlap the psi plane
@@ -316,10 +449,25 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
                 cp_async_wait<0>();
             }
             stage_reduce(m + R);
+        } else if (HALO_ASYNC) {
+            halo_reduce(m + R);
+            if (m + 1 < m1) halo_issue(m + R + 1);
         } else {
             psi_plane(m + R);
         }
         __syncthreads();
+        if constexpr (OWN_TMA) {
+            // buffer of plane m+1 was last read for plane m-1, before the barrier
+            if (m + 1 < m1) own_issue(m + 1);
+            const unsigned k = (*k_wait)++;
+            const int b = k & 1;
+            mbar_wait_bounded(&bars[b], (k >> 1) & 1, err, *dead);
+            if (in_tile) {
+                const float *ob = own + b * (SH::OWN_BOX_BYTES / 4) + tid;
+#pragma unroll
+                for (int q = 0; q < Q; q++) f[q] = ob[q * NT];
+            }
+        }
         if (in_tile) {
             // slot bases of planes m-R .. m+R, offset to this thread's halo position
             const float *sb[RING];
@@ -440,6 +588,46 @@ __global__ void __launch_bounds__(FusedShape<L, S>::NT, MRT ? 2 : (PAIRS ? 4 : 3
         const int m0 = ic * fg.chunk;
         fused_tile<L, S, MRT, void, false, PAIRS>(pop, pop_out, (int)fg.V, fg.L[0], fg.L[1], fg.L[2], ix * SH::TX,
                                                   iy * SH::TY, m0, min(m0 + fg.chunk, Lm), p.neg_g, p.rho0, p, smem);
+    }
+}
+
+// Staged variants of the 3D paired single pass (STG_* flags, BGK): four CTAs
+// per SM with one kind of staging (43 KB or 49 KB of shared memory each), two
+// with both (83 KB).  Shared memory is aligned up to 128 bytes at run time
+// (the TMA destinations), so the launch asks for 128 bytes more than the layout.
+template <class L, class S, bool MRT, int STG>
+__global__ void __launch_bounds__(FusedShape<L, S>::NT,
+                                  ((STG & STG_OWN_TMA) && (STG & STG_HALO_ASYNC)) ? 2 : 4)
+    k_fused_stg(const float *__restrict__ pop, float *__restrict__ pop_out,
+                const __grid_constant__ StepParams<L, S, float> p, const FusedGeom fg,
+                const __grid_constant__ CUtensorMap tmap) {
+    using SH = FusedShape<L, S>;
+    constexpr int D = L::D;
+    extern __shared__ float smem_raw[];
+    float *smem = smem_raw + ((128u - (smem_u32(smem_raw) & 127u)) & 127u) / 4;
+    uint64_t *bars =
+        reinterpret_cast<uint64_t *>(reinterpret_cast<char *>(smem) + SH::own_offset(STG) + 2 * SH::OWN_BOX_BYTES);
+    if constexpr ((STG & STG_OWN_TMA) != 0) {
+        if (threadIdx.x == 0) {
+            mbar_init(&bars[0], 1);
+            mbar_init(&bars[1], 1);
+            mbar_fence_init();
+        }
+        __syncthreads();
+    }
+    unsigned k_issue = 0, k_wait = 0;
+    bool dead = false;
+    const int Lm = D == 3 ? fg.L[2] : fg.L[1];
+    for (int item = blockIdx.x; item < fg.items; item += gridDim.x) {
+        const int ix = item % fg.tiles_x;
+        const int rest = item / fg.tiles_x;
+        const int iy = rest % fg.tiles_y;
+        const int ic = rest / fg.tiles_y;
+        const int m0 = ic * fg.chunk;
+        fused_tile<L, S, MRT, void, false, true, STG>(pop, pop_out, (int)fg.V, fg.L[0], fg.L[1], fg.L[2],
+                                                      ix * SH::TX, iy * SH::TY, m0, min(m0 + fg.chunk, Lm), p.neg_g,
+                                                      p.rho0, p, smem, nullptr, nullptr, nullptr, nullptr, &tmap,
+                                                      bars, &k_issue, &k_wait, fg.err, &dead);
     }
 }
 

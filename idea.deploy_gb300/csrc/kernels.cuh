@@ -228,21 +228,28 @@ __device__ __forceinline__ double strict_term(int k, double c, double n, const d
 // monomials in the reference's print order: d_psi_a (then d_psi_a*lu_0_b), ln_0,
 // ln_0*lu_0_a (then ln_0*lu_0_a*lu_0_b, b >= a)
 template <int D>
+struct PrintOrder {
+    int v[Mono<D>::K];
+    constexpr PrintOrder() : v() {
+        using M = Mono<D>;
+        int pos = 0;
+        for (int a = 0; a < D; a++) {
+            v[pos++] = M::F + a;
+            for (int b = 0; b < D; b++) v[pos++] = M::FU + a * D + b;
+        }
+        v[pos++] = 0;
+        for (int a = 0; a < D; a++) {
+            v[pos++] = M::NU + a;
+            for (int b = a; b < D; b++) v[pos++] = M::nuu(a, b);
+        }
+    }
+};
+// (a table built once by the front end: a search per unrolled use would be
+// folded again at every call site by the device compiler)
+template <int D>
 SCLBM_HD constexpr int print_order(int i) {
-    using M = Mono<D>;
-    int pos = 0;
-    for (int a = 0; a < D; a++) {
-        if (pos++ == i) return M::F + a;
-        for (int b = 0; b < D; b++)
-            if (pos++ == i) return M::FU + a * D + b;
-    }
-    if (pos++ == i) return 0;
-    for (int a = 0; a < D; a++) {
-        if (pos++ == i) return M::NU + a;
-        for (int b = a; b < D; b++)
-            if (pos++ == i) return M::nuu(a, b);
-    }
-    return -1;
+    constexpr PrintOrder<D> t{};
+    return t.v[i];
 }
 
 // Guo-shifted velocity: u = (sum_q xi_q f_q + F/2) / n
@@ -381,13 +388,26 @@ __global__ void __launch_bounds__(128) k_fcs(const Real *__restrict__ pop, Real 
 // stale), so the total mass stays constant.
 // ---------------------------------------------------------------------------
 template <class L>
-SCLBM_HD constexpr int opposite_q(int q) {
-    for (int k = 0; k < L::Q; k++) {
-        bool same = true;
-        for (int d = 0; d < L::D; d++) same = same && (L::xi(k, d) == -L::xi(q, d));
-        if (same) return k;
+struct OppositeQ {
+    int v[L::Q];
+    constexpr OppositeQ() : v() {
+        for (int q = 0; q < L::Q; q++) {
+            v[q] = q;
+            for (int k = 0; k < L::Q; k++) {
+                bool same = true;
+                for (int d = 0; d < L::D; d++) same = same && (L::xi(k, d) == -L::xi(q, d));
+                if (same) {
+                    v[q] = k;
+                    break;
+                }
+            }
+        }
     }
-    return q;
+};
+template <class L>
+SCLBM_HD constexpr int opposite_q(int q) {
+    constexpr OppositeQ<L> t{};
+    return t.v[q];
 }
 
 template <class L, class Real>

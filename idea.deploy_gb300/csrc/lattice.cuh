@@ -135,20 +135,33 @@ struct Mono {
 // Is the BGK coefficient of monomial k for population q nonzero?  Fixed by
 // the lattice vector alone (w_q > 0, xi^2 - c2 != 0 for c2 = 1/3).
 template <class L>
-SCLBM_HD constexpr bool bgk_nonzero(int q, int k) {
-    constexpr int D = L::D;
-    using M = Mono<D>;
-    if (k == 0) return true;
-    if (k < M::NUU) return L::xi(q, k - M::NU) != 0;
-    if (k < M::F) {
-        for (int a = 0; a < D; a++)
-            for (int b = a; b < D; b++)
-                if (M::nuu(a, b) == k) return a == b ? true : (L::xi(q, a) * L::xi(q, b) != 0);
-        return false;
+struct BgkNonzero {
+    bool v[L::Q][Mono<L::D>::K];
+    constexpr BgkNonzero() : v() {
+        constexpr int D = L::D;
+        using M = Mono<D>;
+        for (int q = 0; q < L::Q; q++)
+            for (int k = 0; k < M::K; k++) {
+                bool nz = false;
+                if (k == 0) nz = true;
+                else if (k < M::NUU) nz = L::xi(q, k - M::NU) != 0;
+                else if (k < M::F) {
+                    for (int a = 0; a < D; a++)
+                        for (int b = a; b < D; b++)
+                            if (M::nuu(a, b) == k) nz = a == b ? true : (L::xi(q, a) * L::xi(q, b) != 0);
+                } else if (k < M::FU) nz = L::xi(q, k - M::F) != 0;
+                else {
+                    const int a = (k - M::FU) / D, b = (k - M::FU) % D;
+                    nz = a == b ? true : (L::xi(q, a) * L::xi(q, b) != 0);
+                }
+                v[q][k] = nz;
+            }
     }
-    if (k < M::FU) return L::xi(q, k - M::F) != 0;
-    const int a = (k - M::FU) / D, b = (k - M::FU) % D;
-    return a == b ? true : (L::xi(q, a) * L::xi(q, b) != 0);
+};
+template <class L>
+SCLBM_HD constexpr bool bgk_nonzero(int q, int k) {
+    constexpr BgkNonzero<L> t{};
+    return t.v[q][k];
 }
 
 }  // namespace sclbm

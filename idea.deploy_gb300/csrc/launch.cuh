@@ -54,10 +54,13 @@ struct KernelOps {
     // occupancy-derived grid sizes (blocks) for a device with `sms` SMs
     void (*grids)(int sms, int *density_grid, int *fcs_grid);
     // single-pass step (FP32 only, else null): launcher, tile shape, resident CTAs per SM
+    // tmap: host copy of the input buffer's CUtensorMap (used when fg.stg has STG_OWN_TMA)
     cudaError_t (*fused)(const void *pop, void *pop_out, const void *step_params, const FusedGeom &fg, int grid,
-                         cudaStream_t st);
+                         const void *tmap, cudaStream_t st);
     int fused_tx, fused_ty, fused_r;
-    int (*fused_occupancy)(int pairs);  // of the paired-load instance when pairs != 0
+    int (*fused_occupancy)(int pairs, int stg);  // of the paired-load instance when pairs != 0
+    int fused_stg_mask;                          // STG_* variants built for this kernel set (0: none)
+    int (*fused_smem)(int pairs, int stg);       // dynamic shared memory of a launch
     // batches of lattices (FP32 only, else null)
     cudaError_t (*batch_step)(const void *pop, void *pop_out, const void *sp, const BatchInst *inst, const int4 *items,
                               int n_items, int Vtot, int *counter, int parity, int pairs, int grid, cudaStream_t st);
@@ -189,11 +192,45 @@ struct Ops {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fcs<L, S, MRT, Real, STRICT>, 128, 0);
         *fg = sms * (b > 0 ? b : 1);
     }
+    // staged variants: 3D, even radius, BGK, FP32
+    static constexpr bool STG_BUILT = std::is_same<Real, float>::value && L::D == 3 && S::R % 2 == 0 && !MRT;
+    static constexpr int STG_MASK = STG_BUILT ? 3 : 0;
+    static int fused_smem(int pairs, int stg) {
+        using SH = FusedShape<L, S>;
+        if (pairs && stg) return SH::stg_smem(stg) + 128;
+        return SH::SMEM;
+    }
+    template <int STG>
+    static cudaError_t launch_stg(const void *pop, void *pop_out, const void *sp, const FusedGeom &fg, int grid,
+                                  const void *tmap, cudaStream_t st) {
+        using SH = FusedShape<L, S>;
+        static bool done[64] = {};
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (dev < 0 || dev >= 64 || !done[dev]) {
+            cudaFuncSetAttribute(k_fused_stg<L, S, MRT, STG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 SH::stg_smem(STG) + 128);
+            if (dev >= 0 && dev < 64) done[dev] = true;
+        }
+        if (!tmap && (STG & STG_OWN_TMA)) return cudaErrorInvalidValue;
+        CUtensorMap none;
+        std::memset(&none, 0, sizeof(none));
+        k_fused_stg<L, S, MRT, STG><<<grid, SH::NT, SH::stg_smem(STG) + 128, st>>>(
+            (const float *)pop, (float *)pop_out, *static_cast<const SP *>(sp), fg,
+            tmap ? *static_cast<const CUtensorMap *>(tmap) : none);
+        return cudaGetLastError();
+    }
     static cudaError_t fused(const void *pop, void *pop_out, const void *sp, const FusedGeom &fg, int grid,
-                             cudaStream_t st) {
+                             const void *tmap, cudaStream_t st) {
         if constexpr (std::is_same<Real, float>::value) {
             using SH = FusedShape<L, S>;
             allow_smem();
+            if constexpr (STG_BUILT) {
+                if (fg.pairs && fg.stg == 1) return launch_stg<1>(pop, pop_out, sp, fg, grid, tmap, st);
+                if (fg.pairs && fg.stg == 2) return launch_stg<2>(pop, pop_out, sp, fg, grid, tmap, st);
+                if (fg.pairs && fg.stg == 3) return launch_stg<3>(pop, pop_out, sp, fg, grid, tmap, st);
+            }
+            if (fg.stg) return cudaErrorNotSupported;
             if constexpr (L::D == 3 && S::R % 2 == 0) {
                 if (fg.pairs) {
                     k_fused<L, S, MRT, true><<<grid, SH::NT, SH::SMEM, st>>>((const float *)pop, (float *)pop_out,
@@ -223,10 +260,24 @@ struct Ops {
             }
         }
     }
-    static int fused_occupancy(int pairs) {
+    template <int STG>
+    static int occupancy_stg() {
+        using SH = FusedShape<L, S>;
+        cudaFuncSetAttribute(k_fused_stg<L, S, MRT, STG>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             SH::stg_smem(STG) + 128);
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fused_stg<L, S, MRT, STG>, SH::NT, SH::stg_smem(STG) + 128);
+        return b > 0 ? b : 1;
+    }
+    static int fused_occupancy(int pairs, int stg) {
         if constexpr (std::is_same<Real, float>::value) {
             using SH = FusedShape<L, S>;
             allow_smem();
+            if constexpr (STG_BUILT) {
+                if (pairs && stg == 1) return occupancy_stg<1>();
+                if (pairs && stg == 2) return occupancy_stg<2>();
+                if (pairs && stg == 3) return occupancy_stg<3>();
+            }
             int b = 0;
             if constexpr (L::D == 3 && S::R % 2 == 0) {
                 if (pairs) {
@@ -496,7 +547,7 @@ struct Ops {
         static const KernelOps o = {sizeof(SP), sizeof(EP), f32 ? 1 : 2, &fill_step, &fill_eq, &density,
                                     &fcs, &velocity, &density_walls, &fcs_walls, &init_pop, &grids,
                                     f32 ? &fused : nullptr, SH::TX, SH::TY, SH::R,
-                                    f32 ? &fused_occupancy : nullptr,
+                                    f32 ? &fused_occupancy : nullptr, STG_MASK, &fused_smem,
                                     f32 ? &batch_step : nullptr, f32 ? &batch_density : nullptr,
                                     f32 ? &batch_moments : nullptr, f32 ? &batch_mass : nullptr,
                                     f32 ? &batch_add_rest : nullptr, f32 ? &batch_probe : nullptr,

@@ -2,14 +2,17 @@
 // the step loop (CUDA-graph replay of the two-pass step), read-back and the FP64
 // reductions.
 #include <algorithm>
+#include <array>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <string>
 #include <vector>
 
+#include <cuda.h>  // CUcontext / CUresult types; the entry points come from the runtime
 #include <cuda_runtime.h>
 
 #include "../../include/sclbm.h"
@@ -251,6 +254,12 @@ struct sclbm_sim {
     int dgrid = 0, fgrid = 0, ugrid = 0;
     FusedGeom fg = {};
     int fused_grid = 0, path = SCLBM_PATH_AUTO, chunk_override = 0;
+    int staging = -1;  // requested SCLBM_STAGE_* flags of the 3D single pass (-1: automatic)
+    // tensor maps of the two population buffers (4D: x, y, plane, q; box of one
+    // tile plane), encoded when a staged variant with TMA loads is planned
+    CUtensorMap tmap[2];
+    bool tmap_ok = false;
+    int *flag_host = nullptr, *flag_dev = nullptr;  // set by a device wait that gave up (mapped pinned int)
     bool n_set = false, u_set = false, pop_set = false, moments_fresh = false;
     bool dn_fresh = true;  // dn holds the density of the current populations
     cudaGraphExec_t graph[2] = {nullptr, nullptr};
@@ -294,6 +303,7 @@ void release(sclbm_sim *s) {
     for (auto &ev : s->stage_ev)
         if (ev) cudaEventDestroy(ev), ev = nullptr;
     if (s->stage) cudaFreeHost(s->stage);
+    if (s->flag_host) cudaFreeHost(s->flag_host);
     if (s->st) cudaStreamDestroy(s->st);
 }
 
@@ -432,7 +442,8 @@ int launch_step(sclbm_sim *s, cudaEvent_t *ev = nullptr) {
             e = o->fused_noise(s->pop[s->cur], s->pop[s->cur ^ 1], s->sp.data(), s->fg, s->seeds, s->np.data(),
                                s->fused_grid, s->st);
         else
-            e = o->fused(s->pop[s->cur], s->pop[s->cur ^ 1], s->sp.data(), s->fg, s->fused_grid, s->st);
+            e = o->fused(s->pop[s->cur], s->pop[s->cur ^ 1], s->sp.data(), s->fg, s->fused_grid,
+                         (s->fg.stg & STG_OWN_TMA) ? (const void *)&s->tmap[s->cur] : nullptr, s->st);
         if (ev && e == cudaSuccess) e = cudaEventRecord(ev[0], s->st);
     } else {
         e = density_pass(s);
@@ -452,12 +463,104 @@ int launch_step(sclbm_sim *s, cudaEvent_t *ev = nullptr) {
     return SCLBM_OK;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no link
+// to the driver library)
+using PfnEncodeTiled = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                    const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                    CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+PfnEncodeTiled encode_tiled() {
+    static PfnEncodeTiled fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PfnEncodeTiled>(f);
+        cudaGetLastError();
+    });
+    return fn;
+}
+
+// the population buffers as 4D FP32 tensors (x, y, plane, q) with a box of one
+// tile plane (TX, TY, 1, Q); TMA needs 16-byte strides, so Lx % 4 == 0
+bool encode_tmaps(sclbm_sim *s) {
+    const KernelOps *o = s->ops;
+    if (s->D != 3 || s->L[0] % 4 != 0) return false;
+    PfnEncodeTiled enc = encode_tiled();
+    if (!enc) return false;
+    const cuuint64_t dims[4] = {(cuuint64_t)s->L[0], (cuuint64_t)s->L[1], (cuuint64_t)s->L[2], (cuuint64_t)s->Q};
+    const cuuint64_t strides[3] = {(cuuint64_t)s->L[0] * 4, (cuuint64_t)s->L[0] * s->L[1] * 4, (cuuint64_t)s->V * 4};
+    const cuuint32_t box[4] = {(cuuint32_t)o->fused_tx, (cuuint32_t)o->fused_ty, 1, (cuuint32_t)s->Q};
+    const cuuint32_t unit[4] = {1, 1, 1, 1};
+    for (int b = 0; b < 2; b++) {
+        if (enc(&s->tmap[b], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, s->pop[b], dims, strides, box, unit,
+                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+            return false;
+    }
+    return true;
+}
+
+// staging of the 3D single pass: the requested flags where the kernel set has
+// them and the box supports them; automatic (-1): none until measured
+int plan_staging(sclbm_sim *s, bool pairs) {
+    if (!pairs || s->walls || s->noise_kind || s->staging <= 0) return 0;
+    int stg = s->staging & s->ops->fused_stg_mask;
+    if (stg & STG_OWN_TMA) {
+        if (!s->tmap_ok) s->tmap_ok = encode_tmaps(s);
+        if (!s->tmap_ok) stg &= ~STG_OWN_TMA;
+    }
+    return stg;
+}
+
+// ---- tuned configurations, cached per (lattice, stencil, operator, box, device) ----
+// the kernel set (lattice, stencil, operator kind, precision, arithmetic) is
+// identified by its KernelOps table; walls, box and SM count complete the key
+struct TuneKey {
+    const KernelOps *ops;
+    int v[6];
+    bool operator<(const TuneKey &o) const {
+        if (ops != o.ops) return std::less<const KernelOps *>()(ops, o.ops);
+        return std::lexicographical_compare(v, v + 6, o.v, o.v + 6);
+    }
+};
+std::mutex g_tune_mu;
+std::map<TuneKey, sclbm_tuning> g_tune_cache;
+
+TuneKey tune_key(const sclbm_sim *s) {
+    return TuneKey{s->ops, {s->walls ? 1 : 0, s->noise_kind, s->L[0], s->L[1], s->L[2], s->sms}};
+}
+
+bool cached_tuning(const sclbm_sim *s, sclbm_tuning *t) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tune_cache.find(tune_key(s));
+    if (it == g_tune_cache.end()) return false;
+    *t = it->second;
+    return true;
+}
+
 // work decomposition of the single-pass kernel: tiles of the leading
 // dimensions x chunks of the marching dimension, sized so the items fill the
-// resident CTAs in whole waves with a small halo-plane overhead per chunk
+// resident CTAs in whole waves with a small halo-plane overhead per chunk.
+// A handle left on the automatic choice (path AUTO, no chunk, staging -1)
+// takes the configuration sclbm_autotune found for its key, if any.
 void plan_fused(sclbm_sim *s) {
     const KernelOps *o = s->ops;
     if (!o->fused) return;
+    sclbm_tuning tuned;
+    if (s->path == SCLBM_PATH_AUTO && s->chunk_override == 0 && s->staging < 0 && cached_tuning(s, &tuned)) {
+        const int saved_path = s->path, saved_chunk = s->chunk_override, saved_stg = s->staging;
+        s->path = tuned.path == SCLBM_PATH_FUSED ? SCLBM_PATH_FUSED : SCLBM_PATH_AUTO;
+        s->chunk_override = tuned.chunk;
+        s->staging = tuned.staging;
+        plan_fused(s);
+        s->path = saved_path;
+        s->chunk_override = saved_chunk;
+        s->staging = saved_stg;
+        return;
+    }
     FusedGeom &g = s->fg;
     for (int d = 0; d < 3; d++) g.L[d] = d < s->D ? s->L[d] : 1;
     g.V = s->V;
@@ -468,9 +571,11 @@ void plan_fused(sclbm_sim *s) {
     // than one cell per load at 256^3 D3Q19 E6/E8, bit-identical results)
     g.pairs = (s->path == SCLBM_PATH_FUSED_PAIRS || s->path == SCLBM_PATH_AUTO) && s->D == 3 && s->L[0] % 2 == 0 &&
               o->fused_r % 2 == 0;
+    g.stg = plan_staging(s, g.pairs);
+    g.err = s->flag_dev;
     const int resident = s->sms * (s->noise_kind ? o->fused_noise_occupancy()
                                    : s->walls    ? o->fused_walls_occupancy()
-                                                 : o->fused_occupancy(g.pairs));
+                                                 : o->fused_occupancy(g.pairs, g.stg));
     const int base = g.tiles_x * g.tiles_y;
     int best_c = 1;
     double best = -1;
@@ -924,6 +1029,18 @@ int sclbm_create(const sclbm_params *p, sclbm_sim **out) {
     s->red_blocks = prop.multiProcessorCount * 2;
     if (!rc) rc = alloc(s, (void **)&s->red, (size_t)s->red_blocks * 8 * sizeof(double));
     if (!rc) {
+        // a host int the kernels can write (mapped pinned memory): the flag of
+        // a bounded device wait that gave up, read after every synchronisation
+        if (cudaHostAlloc((void **)&s->flag_host, sizeof(int), cudaHostAllocMapped) != cudaSuccess ||
+            cudaHostGetDevicePointer((void **)&s->flag_dev, s->flag_host, 0) != cudaSuccess) {
+            cudaGetLastError();
+            rc = fail(SCLBM_ERR_CUDA, "mapped flag");
+        } else {
+            *s->flag_host = 0;
+            s->fg.err = s->flag_dev;
+        }
+    }
+    if (!rc) {
         if (cudaMemsetAsync(s->u, 0, fb * s->D, s->st) != cudaSuccess ||
             cudaMemsetAsync(s->u_old, 0, fb * s->D, s->st) != cudaSuccess ||
             cudaMemsetAsync(s->dn, 0, fb, s->st) != cudaSuccess ||
@@ -1058,11 +1175,21 @@ int sclbm_step(sclbm_sim *s, int64_t nsteps) {
     return rc;
 }
 
+// after a synchronisation: a staged kernel's bounded wait that gave up
+int check_flag(sclbm_sim *s) {
+    if (s->flag_host && *(volatile int *)s->flag_host) {
+        *s->flag_host = 0;
+        return fail(SCLBM_ERR_CUDA, "a staged single-pass kernel gave up waiting for its TMA loads "
+                                    "(results of the last steps are invalid)");
+    }
+    return SCLBM_OK;
+}
+
 int sclbm_sync(sclbm_sim *s) {
     if (!s) return fail(SCLBM_ERR_ARG, "null handle");
     DevGuard dg(s->device);
     CUDA_TRY(cudaStreamSynchronize(s->st));
-    return SCLBM_OK;
+    return check_flag(s);
 }
 
 int sclbm_step_timed(sclbm_sim *s, int64_t nsteps, double *ms) {
@@ -1084,7 +1211,7 @@ int sclbm_step_timed(sclbm_sim *s, int64_t nsteps, double *ms) {
     *ms = t;
     if (rc) return rc;
     CUDA_TRY(cudaGetLastError());
-    return SCLBM_OK;
+    return check_flag(s);
 }
 
 int sclbm_profile_step(sclbm_sim *s, int64_t nsteps, double *ms, int nms) {
@@ -1118,6 +1245,7 @@ int sclbm_profile_step(sclbm_sim *s, int64_t nsteps, double *ms, int nms) {
     s->moments_fresh = s->dn_fresh = false;
     if (rc) return rc;
     if (ce != cudaSuccess) return fail(SCLBM_ERR_CUDA, "profile: %s", cudaGetErrorString(ce));
+    if ((rc = check_flag(s))) return rc;
     ms[0] = t0 / nsteps;  // density + psi pass (0 on the single-pass path)
     ms[1] = t1 / nsteps;  // force + collide + stream (the whole step on the single-pass path)
     return SCLBM_OK;
@@ -1151,6 +1279,135 @@ int sclbm_get_tuning(const sclbm_sim *s, int *path, int *chunk, int *grid) {
                                              : SCLBM_PATH_FUSED;
     if (chunk) *chunk = fused_path(s) ? s->fg.chunk : 0;
     if (grid) *grid = fused_path(s) ? s->fused_grid : s->fgrid;
+    return SCLBM_OK;
+}
+
+int sclbm_set_tuning_ex(sclbm_sim *s, const sclbm_tuning *t) {
+    if (!s || !t) return fail(SCLBM_ERR_ARG, "null argument");
+    if (t->staging < -1 || t->staging > (SCLBM_STAGE_HALO_ASYNC | SCLBM_STAGE_OWN_TMA))
+        return fail(SCLBM_ERR_ARG, "staging %d", t->staging);
+    const int saved = s->staging;
+    s->staging = t->staging;
+    const int rc = sclbm_set_tuning(s, t->path, t->chunk);
+    if (rc) s->staging = saved;
+    return rc;
+}
+
+int sclbm_get_tuning_ex(const sclbm_sim *s, sclbm_tuning *t) {
+    if (!s || !t) return fail(SCLBM_ERR_ARG, "null argument");
+    sclbm_get_tuning(s, &t->path, &t->chunk, &t->grid);
+    t->staging = fused_path(s) ? s->fg.stg : 0;
+    return SCLBM_OK;
+}
+
+// Autotuner (no counterpart in the reference, whose generated kernels run a
+// fixed 128-thread block, idpy/LBM/MultiPhase.py:2072-2085).  Candidates are
+// the variants of the handle's current step that compute bit-identical
+// results: on the single pass, one or two halo cells per load, the staging
+// flags and the chunk length (planes each CTA marches, i.e. cells per thread
+// along the marching axis); the two-pass path has no variants.  Each is timed
+// with CUDA events on the handle's stream over trial_steps launches that all
+// read the current populations and write the other buffer (the state is left
+// as it was); the fastest is applied and cached for this key.
+int sclbm_autotune(sclbm_sim *s, int trial_steps, sclbm_tuning *best, double *best_ms) {
+    if (!s) return fail(SCLBM_ERR_ARG, "null handle");
+    if (trial_steps < 1 || trial_steps > 10000) return fail(SCLBM_ERR_ARG, "trial_steps in [1, 10000]");
+    if (!s->pop_set) return fail(SCLBM_ERR_STATE, "populations are not initialized");
+    if (s->noise_kind)
+        return fail(SCLBM_ERR_UNSUPPORTED, "fluctuating handles are not tuned (a trial step would advance the "
+                                           "generator states)");
+    if (s->simple_mode)
+        return fail(SCLBM_ERR_UNSUPPORTED, "the simple step family is not tuned (its inlet/outlet kernels "
+                                           "write the current populations)");
+    DevGuard dg(s->device);
+    CUDA_TRY(cudaStreamSynchronize(s->st));
+    const int saved_path = s->path, saved_chunk = s->chunk_override, saved_stg = s->staging;
+    struct Cand {
+        int path, chunk, staging;
+    };
+    std::vector<Cand> cands;
+    if (!fused_path(s)) {
+        cands.push_back({s->path, 0, 0});
+    } else {
+        const int Lm = s->D == 3 ? s->L[2] : s->L[1];
+        const bool pairs_ok = s->D == 3 && s->L[0] % 2 == 0 && s->ops->fused_r % 2 == 0 && !s->walls;
+        std::vector<int> chunks = {0};
+        for (int c : {8, 12, 16, 24, 32, 40, 48, 64, 96, 128})
+            if (c < Lm) chunks.push_back(c);
+        std::vector<int> paths = {SCLBM_PATH_FUSED};
+        if (pairs_ok) paths.insert(paths.begin(), SCLBM_PATH_FUSED_PAIRS);
+        for (int path : paths)
+            for (int stg = 0; stg <= 3; stg++) {
+                if (stg && (path != SCLBM_PATH_FUSED_PAIRS || !(s->ops->fused_stg_mask & stg))) continue;
+                for (int c : chunks) cands.push_back({path, c, stg});
+            }
+    }
+    cudaEvent_t e0, e1;
+    CUDA_TRY(cudaEventCreate(&e0));
+    CUDA_TRY(cudaEventCreate(&e1));
+    double best_t = 1e300;
+    Cand win = cands[0];
+    std::vector<std::array<int, 4>> seen;  // effective (pairs, staging, chunk, grid) already timed
+    int rc = SCLBM_OK;
+    for (const Cand &c : cands) {
+        s->path = c.path;
+        s->chunk_override = c.chunk;
+        s->staging = c.staging;
+        plan_fused(s);
+        const std::array<int, 4> eff = {fused_path(s) ? s->fg.pairs : -1, fused_path(s) ? s->fg.stg : -1,
+                                        fused_path(s) ? s->fg.chunk : 0, fused_path(s) ? s->fused_grid : 0};
+        if (std::find(seen.begin(), seen.end(), eff) != seen.end()) continue;
+        seen.push_back(eff);
+        // one untimed launch, then trial_steps timed ones, all from the current buffer
+        for (int i = 0; i <= trial_steps && rc == SCLBM_OK; i++) {
+            if (i == 1) cudaEventRecord(e0, s->st);
+            rc = launch_step(s);
+            s->cur ^= 1;
+        }
+        cudaEventRecord(e1, s->st);
+        const cudaError_t ce = cudaEventSynchronize(e1);
+        if (rc == SCLBM_OK && ce != cudaSuccess) rc = fail(SCLBM_ERR_CUDA, "autotune: %s", cudaGetErrorString(ce));
+        if (rc == SCLBM_OK) rc = check_flag(s);
+        if (rc) break;
+        float ms = 0;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best_t) {
+            best_t = ms;
+            win = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    s->moments_fresh = s->dn_fresh = false;
+    if (rc) {
+        s->path = saved_path;
+        s->chunk_override = saved_chunk;
+        s->staging = saved_stg;
+        plan_fused(s);
+        return rc;
+    }
+    s->path = win.path;
+    s->chunk_override = win.chunk;
+    s->staging = win.staging;
+    plan_fused(s);
+    for (auto &g : s->graph)
+        if (g) cudaGraphExecDestroy(g), g = nullptr;
+    sclbm_tuning t = {};
+    sclbm_get_tuning_ex(s, &t);
+    t.chunk = win.chunk;  // 0: the planner's choice won (re-planned for the box)
+    t.path = win.path;
+    {
+        std::lock_guard<std::mutex> lk(g_tune_mu);
+        g_tune_cache[tune_key(s)] = t;
+    }
+    if (best) sclbm_get_tuning_ex(s, best);
+    if (best_ms) *best_ms = best_t / trial_steps;
+    return SCLBM_OK;
+}
+
+int sclbm_clear_tuning_cache(void) {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tune_cache.clear();
     return SCLBM_OK;
 }
 
@@ -1600,7 +1857,7 @@ void batch_items(const sclbm_batch *b, int chunk, std::vector<int4> &items) {
 }
 
 int batch_plan(sclbm_batch *b) {
-    const int resident = b->sms * b->ops->fused_occupancy(0);
+    const int resident = b->sms * b->ops->fused_occupancy(0, 0);
     int chunk = BATCH_CHUNK;
     std::vector<int4> items;
     batch_items(b, chunk, items);
@@ -2039,23 +2296,68 @@ namespace {
 
 constexpr int NOALLOC_MAX_DEVICES = 64;
 std::mutex g_noalloc_mu;
-void *g_noalloc_addr[NOALLOC_MAX_DEVICES] = {};
 
-// device address of the scratch array on the current device (looked up once
-// per device; the host-side symbol itself is not a device address)
+// The array's device address belongs to the CUDA context the library's module
+// was loaded in.  A cudaDeviceReset (a new primary context) or a caller's own
+// current context loads the module again, possibly elsewhere, so the cache
+// holds the address together with the id of the context it was taken in
+// (cuCtxGetId: unique for the life of the process, never reused).
+struct NoallocSlot {
+    unsigned long long ctx_id;
+    void *addr;
+};
+NoallocSlot g_noalloc_slot[NOALLOC_MAX_DEVICES] = {};
+
+using PfnCtxGetCurrent = CUresult (*)(CUcontext *);
+using PfnCtxGetId = CUresult (*)(CUcontext, unsigned long long *);
+PfnCtxGetCurrent g_ctx_get_current = nullptr;
+PfnCtxGetId g_ctx_get_id = nullptr;
+
+// id of the context current on this thread (the runtime made the device's
+// primary context current in DevGuard unless the caller has its own current)
+int current_context_id(unsigned long long *id) {
+    if (!g_ctx_get_current || !g_ctx_get_id) {
+        cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+        void *f1 = nullptr, *f2 = nullptr;
+        const cudaError_t e1 = cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f1, 12000, cudaEnableDefault, &q1);
+        const cudaError_t e2 = cudaGetDriverEntryPointByVersion("cuCtxGetId", &f2, 12000, cudaEnableDefault, &q2);
+        if (e1 != cudaSuccess || e2 != cudaSuccess || q1 != cudaDriverEntryPointSuccess ||
+            q2 != cudaDriverEntryPointSuccess || !f1 || !f2) {
+            cudaGetLastError();
+            return fail(SCLBM_ERR_CUDA, "driver entry points cuCtxGetCurrent/cuCtxGetId not available");
+        }
+        g_ctx_get_current = reinterpret_cast<PfnCtxGetCurrent>(f1);
+        g_ctx_get_id = reinterpret_cast<PfnCtxGetId>(f2);
+    }
+    CUcontext c = nullptr;
+    if (g_ctx_get_current(&c) != CUDA_SUCCESS || !c) return fail(SCLBM_ERR_CUDA, "no current CUDA context");
+    if (g_ctx_get_id(c, id) != CUDA_SUCCESS) return fail(SCLBM_ERR_CUDA, "cuCtxGetId failed");
+    return SCLBM_OK;
+}
+
+// device address of the scratch array in the current context of device dev
+// (looked up once per device and context; the host-side symbol itself is not a
+// device address)
 int noalloc_scratch(int dev, void **out) {
     if (dev < 0 || dev >= NOALLOC_MAX_DEVICES) return fail(SCLBM_ERR_ARG, "device %d beyond %d", dev, NOALLOC_MAX_DEVICES);
     std::lock_guard<std::mutex> lk(g_noalloc_mu);
-    if (!g_noalloc_addr[dev]) {
+    unsigned long long id = 0;
+    {
+        const int rc = current_context_id(&id);
+        if (rc) return rc;
+    }
+    NoallocSlot &slot = g_noalloc_slot[dev];
+    if (!slot.addr || slot.ctx_id != id) {
         void *p = nullptr;
         const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
         if (e != cudaSuccess || !p) {
             cudaGetLastError();
             return fail(SCLBM_ERR_CUDA, "cudaGetSymbolAddress(scratch) on device %d: %s", dev, cudaGetErrorString(e));
         }
-        g_noalloc_addr[dev] = p;
+        slot.ctx_id = id;
+        slot.addr = p;
     }
-    *out = g_noalloc_addr[dev];
+    *out = slot.addr;
     return SCLBM_OK;
 }
 
@@ -2104,6 +2406,14 @@ extern "C" int sclbm_step_noalloc(const sclbm_params *p, const void *pop_in, voi
     }
     if (major < 10) return fail(SCLBM_ERR_NODEVICE, "device %d is sm_%dx; built for sm_103a", p->device, major);
     DevGuard dg(p->device);
+    // an error the caller's own work left pending on this thread stays the
+    // caller's: it is neither reported as this step's failure nor cleared
+    {
+        const cudaError_t pend = cudaPeekAtLastError();
+        if (pend != cudaSuccess)
+            return fail(SCLBM_ERR_CUDA, "a CUDA error was already pending before the step (left uncleared): %s",
+                        cudaGetErrorString(pend));
+    }
     void *scratch = nullptr;
     {
         int rc = noalloc_scratch(p->device, &scratch);

@@ -22,6 +22,7 @@ CRNG_KINDS = {'MINSTD': CRNG_MINSTD, 'NUMREC': CRNG_NUMREC, 'MMIX': CRNG_MMIX}
 SEEDS_STREAM_MAJOR, SEEDS_CELL_MAJOR = 0, 1
 SIMPLE_OFF, SIMPLE_GUO, SIMPLE_SC = 0, 1, 2
 TRANSFER_AUTO, TRANSFER_STAGED, TRANSFER_DIRECT = 0, 1, 2
+STAGE_AUTO, STAGE_NONE, STAGE_HALO_ASYNC, STAGE_OWN_TMA = -1, 0, 1, 2
 
 
 class SclbmError(RuntimeError):
@@ -33,6 +34,10 @@ class SclbmError(RuntimeError):
 _STATUS = {OK: 'ok', ERR_ARG: 'invalid argument', ERR_UNSUPPORTED: 'unsupported configuration',
            ERR_CUDA: 'CUDA error', ERR_STATE: 'call out of order', ERR_NOMEM: 'out of device memory',
            ERR_NODEVICE: 'no usable device'}
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [('path', ctypes.c_int), ('chunk', ctypes.c_int), ('staging', ctypes.c_int), ('grid', ctypes.c_int)]
 
 
 class Params(ctypes.Structure):
@@ -118,6 +123,10 @@ SIGNATURES = {
     'sclbm_mlp_gradient': [_P, _I64, _P, _P, _P, _P],
     'sclbm_mlp_predict': [_P, _I64, _P, _P],
     'sclbm_step_noalloc': [ctypes.POINTER(Params), _P, _P, _P],
+    'sclbm_set_tuning_ex': [_P, ctypes.POINTER(Tuning)],
+    'sclbm_get_tuning_ex': [_P, ctypes.POINTER(Tuning)],
+    'sclbm_autotune': [_P, ctypes.c_int, ctypes.POINTER(Tuning), _DP],
+    'sclbm_clear_tuning_cache': [],
 }
 _STR = {'sclbm_version', 'sclbm_status_string', 'sclbm_last_error'}
 
@@ -310,6 +319,23 @@ class Sim:
         call('sclbm_get_tuning', self.h, ctypes.byref(p), ctypes.byref(c), ctypes.byref(g))
         return p.value, c.value, g.value
 
+    def set_tuning_ex(self, path=PATH_AUTO, chunk=0, staging=STAGE_AUTO):
+        t = Tuning(int(path), int(chunk), int(staging), 0)
+        call('sclbm_set_tuning_ex', self.h, ctypes.byref(t))
+
+    def get_tuning_ex(self):
+        """dict(path, chunk, staging, grid) of what runs"""
+        t = Tuning()
+        call('sclbm_get_tuning_ex', self.h, ctypes.byref(t))
+        return dict(path=t.path, chunk=t.chunk, staging=t.staging, grid=t.grid)
+
+    def autotune(self, trial_steps=20):
+        """Time the bit-identical variants of this handle's step, apply and
+        cache the fastest; returns (dict of the configuration, ms per step)."""
+        t, ms = Tuning(), ctypes.c_double()
+        call('sclbm_autotune', self.h, int(trial_steps), ctypes.byref(t), ctypes.byref(ms))
+        return dict(path=t.path, chunk=t.chunk, staging=t.staging, grid=t.grid), ms.value
+
     def info(self):
         v, b = ctypes.c_int64(), ctypes.c_int64()
         call('sclbm_info', self.h, ctypes.byref(v), ctypes.byref(b))
@@ -401,6 +427,10 @@ class Sim:
         f, m = ctypes.c_int(), ctypes.c_double()
         call('sclbm_density_finite', self.h, ctypes.byref(f), ctypes.byref(m))
         return bool(f.value), m.value
+
+
+def clear_tuning_cache():
+    call('sclbm_clear_tuning_cache')
 
 
 def monomial_count(dim):

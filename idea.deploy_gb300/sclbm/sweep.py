@@ -200,11 +200,14 @@ def ragged_sweep(radii, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, che
 
 
 def plain_run(R, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, check_every=500, tol=1e-12,
-              max_steps=200000, noise=0.0, seed=0, device=0, tol_dp=2e-5, patience=4, dim=2, L=None):
+              max_steps=200000, noise=0.0, seed=0, device=0, tol_dp=2e-5, patience=4, dim=2, L=None,
+              stop_at_dp=False):
     """One droplet on the plain FP64 GPU path (exact coefficients), stopped by
     the reference's FP64 criterion u_conv < tol.  The step and wall time at
     which the FP32 batch's criterion (Laplace pressure calm to tol_dp for
-    `patience` checks) would first have stopped it are recorded too."""
+    `patience` checks) would first have stopped it are recorded too; with
+    stop_at_dp the run stops there (the same criterion as the batch; the
+    Laplace pressure is then the mean of the calm checks, as the batch's)."""
     L = L or sweep_geometry([R])[0]
     dims = (L,) * dim
     x, f = XIStencils['D2Q9' if dim == 2 else 'D3Q19'], FStencils[stencil]
@@ -219,7 +222,7 @@ def plain_run(R, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, check_ever
     steps, uc, mu, status = 0, float('nan'), float('nan'), 'max_steps'
     c = L // 2
     probe = [c + L * c + (L * L * c if dim == 3 else 0), s.V - 1]
-    prev, calm, steps_dp, wall_dp = None, 0, None, None
+    prev, calm, steps_dp, wall_dp, hist = None, 0, None, None, []
     while steps < max_steps:
         s.step(check_every)
         steps += check_every
@@ -233,14 +236,21 @@ def plain_run(R, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, check_ever
             dp = laplace_dp(ni, no, G)[0]
             calm = calm + 1 if prev is not None and abs(dp - prev) <= tol_dp * abs(dp) else 0
             prev = dp
+            hist.append(dp)
             if calm >= patience:
                 steps_dp, wall_dp = steps, time.perf_counter() - t0
-        if uc < tol:
+                if stop_at_dp:
+                    status = 'converged'
+                    break
+        if uc < tol and not stop_at_dp:
             status = 'converged'
             break
     ni, no = s.density_at(probe)
     s.close()
-    return dict(R=R, L=L, steps=steps, u_conv=uc, max_u=mu, status=status, dp=laplace_dp(ni, no, G)[0], n_in=ni,
+    dp_end = laplace_dp(ni, no, G)[0]
+    if stop_at_dp and status == 'converged':
+        dp_end = float(np.mean(hist[-patience:]))
+    return dict(R=R, L=L, steps=steps, u_conv=uc, max_u=mu, status=status, dp=dp_end, n_in=ni,
                 n_out=no, wall_s=time.perf_counter() - t0, steps_dp=steps_dp, wall_dp_s=wall_dp)
 
 
@@ -263,7 +273,7 @@ def laplace_fit(G=-4.5, radii=(12, 16, 20, 24, 32, 40, 48), stencil='D2E8', devi
 
 def run_sweep(n=64, r_min=8, seed=2024, G_range=(-6.0, -4.5), stencil='D2E8', check_every=500, tol_dp=2e-5,
               tol64=1e-12, max_steps=100000, coex_steps=200000, plain=True, device=0, init=None, mlp=None,
-              residual_max=0.1):
+              residual_max=0.1, plain_stop_at_dp=False):
     """The ragged droplet sweep: radii r_min .. r_min+n-1, box 4R rounded up to
     32, G uniform in G_range (seeded), densities from the flat-interface runs
     (from the thermodynamic construction where the slab diverged); batched
@@ -323,7 +333,8 @@ def run_sweep(n=64, r_min=8, seed=2024, G_range=(-6.0, -4.5), stencil='D2E8', ch
                 runs.append(None)
                 continue
             runs.append(plain_run(radii[i], float(Gs[i]), rl[i], rg[i], stencil=stencil, check_every=check_every,
-                                  tol=tol64, max_steps=max_steps, device=device))
+                                  tol=tol64, max_steps=max_steps, device=device, tol_dp=tol_dp,
+                                  stop_at_dp=plain_stop_at_dp))
         res['plain'] = runs
         res['plain_wall_s'] = time.perf_counter() - t1
     return res

@@ -260,6 +260,46 @@ SCLBM_API int sclbm_kernels_per_step(const sclbm_sim *s, int *count);
 SCLBM_API int sclbm_set_tuning(sclbm_sim *s, int path, int chunk);
 SCLBM_API int sclbm_get_tuning(const sclbm_sim *s, int *path, int *chunk, int *grid);
 
+/* Staging of the 3D paired single pass (flags; FP32 BGK, E6/E8, even Lx).  No
+ * counterpart in the reference (its generated kernels use a fixed 128-thread
+ * block, idpy/LBM/MultiPhase.py:2072-2085).  The results are bit-identical
+ * with and without staging.
+ *   SCLBM_STAGE_HALO_ASYNC  halo populations of the next plane copied into
+ *                           shared memory with cp.async while a plane collides
+ *   SCLBM_STAGE_OWN_TMA     the tile's own populations of the next plane loaded
+ *                           by one TMA box per plane (needs Lx % 4 == 0) */
+#define SCLBM_STAGE_HALO_ASYNC 1
+#define SCLBM_STAGE_OWN_TMA 2
+/* the kernel configuration of a handle's step: path (SCLBM_PATH_*), chunk
+ * (planes per work item, 0 = planned), staging (SCLBM_STAGE_* flags, -1 =
+ * automatic), grid (CTAs launched; output only).  get reports what runs:
+ * the path and staging that apply to this handle */
+typedef struct sclbm_tuning {
+    int path;
+    int chunk;
+    int staging;
+    int grid;
+} sclbm_tuning;
+SCLBM_API int sclbm_set_tuning_ex(sclbm_sim *s, const sclbm_tuning *t);
+SCLBM_API int sclbm_get_tuning_ex(const sclbm_sim *s, sclbm_tuning *t);
+
+/* Autotuner.  No counterpart in the reference (fixed 128-thread blocks,
+ * idpy/LBM/MultiPhase.py:2072-2085).  Times every variant of the handle's
+ * current step that computes bit-identical results (single pass: one or two
+ * halo cells per load, the staging flags, the chunk length, i.e. the cells
+ * each thread marches; the two-pass path has none) with CUDA events over
+ * trial_steps launches on the handle's stream, applies the fastest and caches
+ * it for the handle's key (lattice, stencil, operator, precision, walls, box,
+ * device SM count); handles created later with that key on the automatic
+ * choice (path AUTO, chunk 0, staging -1) use it.  The trial launches all read
+ * the current populations, so the simulation state is unchanged.  best (may be
+ * NULL) gets the configuration, *best_ms (may be NULL) its time per step.
+ * Fluctuating handles (a trial would advance their generators) and the simple
+ * step family (its inlet/outlet kernels write the current populations) are
+ * refused with SCLBM_ERR_UNSUPPORTED. */
+SCLBM_API int sclbm_autotune(sclbm_sim *s, int trial_steps, sclbm_tuning *best, double *best_ms);
+SCLBM_API int sclbm_clear_tuning_cache(void);
+
 /* observables */
 SCLBM_API int sclbm_compute_moments(sclbm_sim *s);
 /* sum of all populations (FP64 accumulation) and total momentum sum_q xi_q f_q */
@@ -389,8 +429,14 @@ SCLBM_API int sclbm_mlp_predict(sclbm_mlp *m, int64_t n, const float *x, float *
  * device's copy of the array, which keeps the last call's contents, so calls
  * whose kernels overlap on the GPU (streams with no ordering between them)
  * race: order them on one stream.  The first
- * call on each device looks up the array's device address (set-up done once
- * per device); make that first call before any stream capture.
+ * call on each device looks up the array's device address in the context
+ * current on the calling thread (set-up done once per device and context);
+ * a later call that finds another context current (after a cudaDeviceReset,
+ * or with a context the caller made current) looks it up again, since the
+ * array then sits at another address.  Make the first call in each context
+ * before any stream capture.  A CUDA error already pending on the calling
+ * thread when the call starts is reported (SCLBM_ERR_CUDA) and left uncleared,
+ * and nothing is enqueued.
  * ------------------------------------------------------------------------- */
 #define SCLBM_NOALLOC_MAX_CELLS (1 << 20)
 SCLBM_API int sclbm_step_noalloc(const sclbm_params *p, const void *pop_in, void *pop_out, void *stream);

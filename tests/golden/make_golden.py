@@ -88,6 +88,17 @@ DIVERGENCE = dict(xi='D2Q9', fs='D2E4', tau=1.0, G=-5.0, psi='exp', dims=(256, 2
 FULL_TWIN = dict(xi='D2Q9', fs='D2E4', tau=1.0, G=-4.5, psi='exp', dims=(256, 256),
                  R=48.0, rl=4.5625, rg=0.2086, width=2.0, steps=[1000, 10000])
 
+# The 3D headline's shape at a size the reference runs in minutes: D3Q19, E6,
+# MRT with every rate 1.0, a droplet in a 64^3 box at the stable coupling
+# G = -4.5 with the 3D E6 flat-interface densities; 1000 steps.  The radius is
+# 16: a droplet of the headline's proportion (R = 10 here for R = 40 in 256^3)
+# evaporates completely into the small box within 1000 steps (the gas has to
+# take up the Laplace excess, and a small box has too little of it), which
+# would leave a uniform gas to compare.  Compact records (summaries, per-plane
+# sums, two central planes of n and u) keep the fixture small.
+CFG2_64 = dict(xi='D3Q19', fs='D3E6', tau=1.0, G=-4.5, psi='exp', dims=(64, 64, 64),
+               R=16.0, rl=4.636, rg=0.147, width=2.0, steps=[100, 1000], rates=[1.0] * 19)
+
 SEED = 1234
 
 
@@ -293,6 +304,52 @@ def gen_full_twin():
     print('full_twin done in %.1f s' % (time.time() - t0), flush=True)
 
 
+def gen_cfg2_64():
+    c = CFG2_64
+    t0 = time.time()
+    sc = make_sim(c)
+    rho = droplet(c['dims'], c['R'], c['rl'], c['rg'], c['width'])
+    set_fields(sc, rho)
+    rec = {'mass_0': float(sc.sims_idpy_memory['pop'].D2H().sum())}
+    steps = list(c['steps'])
+    state = dict(k=0)
+    L = c['dims'][0]
+    from idpy.LBM.MultiPhaseLoopChecks import CheckUConvergenceSCMP
+
+    def recorder(lbm):
+        k = steps[state['k']]
+        state['k'] += 1
+        lbm.ComputeMomentsMeta()
+        n = lbm.GetDensityField()                                  # (z, y, x)
+        u = lbm.sims_idpy_memory['u'].D2H().reshape(L, L, L, 3)    # (z, y, x, d)
+        rec['mass_%d' % k] = float(lbm.sims_idpy_memory['pop'].D2H().sum())
+        rec['nsum_%d' % k] = float(n.sum())
+        rec['nmax_%d' % k] = float(n.max())
+        rec['nmin_%d' % k] = float(n.min())
+        rec['umax_%d' % k] = float(np.abs(u).max())
+        rec['nplane_%d' % k] = n.sum(axis=(1, 2)).copy()          # per z plane
+        rec['nz_%d' % k] = n[L // 2].copy()                        # plane z = L/2
+        rec['nx_%d' % k] = n[:, :, L // 2 + 3].copy()              # plane x = L/2 + 3
+        rec['uz_%d' % k] = u[L // 2].copy()
+        rec['ux_%d' % k] = u[:, :, L // 2 + 3].copy()
+        with contextlib.redirect_stdout(io.StringIO()):
+            CheckUConvergenceSCMP(lbm)
+        rec['uconv_%d' % k] = float(lbm.sims_vars['u_conv'][-1])
+        rec['maxu_%d' % k] = float(lbm.sims_vars['max_u'][-1])
+        return False
+
+    run_loop(sc, c, steps, recorder)
+    with contextlib.redirect_stdout(io.StringIO()):
+        sc.ComputeMomentsMeta()
+        dp = sc.DeltaPLaplace()
+    rec['dp'] = np.array(dp, dtype=np.float64)
+    rec['seconds'] = time.time() - t0
+    rec['lit_json'] = np.array(json.dumps(parse_literals('K_ForceCollideStreamSCMP_MRTMeta', c)))
+    np.savez_compressed(os.path.join(HERE, 'cfg2_64.npz'), **rec,
+                        config_json=np.array(json.dumps(dict(c, seed=SEED))))
+    print('cfg2_64 done in %.1f s' % (time.time() - t0), flush=True)
+
+
 def gen_init_profiles():
     """The reference's own interface-initialisation kernels (width 1)."""
     rec = {}
@@ -352,7 +409,7 @@ def main():
     ap.add_argument('cases', nargs='*')
     a = ap.parse_args()
     setup_reference(os.path.abspath(a.reference))
-    todo = a.cases or (list(CASES) + ['div_cfg1', 'full_twin_256', 'init_profiles', 'mrt_basis'])
+    todo = a.cases or (list(CASES) + ['div_cfg1', 'full_twin_256', 'cfg2_64', 'init_profiles', 'mrt_basis'])
     for name in todo:
         if name in CASES:
             gen_case(name, CASES[name])
@@ -360,6 +417,8 @@ def main():
             gen_divergence()
         elif name == 'full_twin_256':
             gen_full_twin()
+        elif name == 'cfg2_64':
+            gen_cfg2_64()
         elif name == 'init_profiles':
             gen_init_profiles()
         elif name == 'mrt_basis':

@@ -149,6 +149,31 @@ def test_full_size_twin_1000_steps_vs_oracle():
     sc.End()
 
 
+def test_full_size_twin_10000_steps_vs_reference():
+    """The 2D headline's full run length: 256^2, R=48, G=-4.5, 10,000 steps of
+    the FP64 path in the reference's arithmetic against the reference's own
+    10,000-step record (central row and column of n, a row of u, extrema,
+    density sum and mass)."""
+    z, cfg = load('full_twin_256')
+    n0 = droplet(cfg['dims'], cfg['R'], cfg['rl'], cfg['rg'], cfg['width'], cfg['seed'])
+    sc = make_gpu(cfg)
+    set_droplet(sc, n0)
+    sc.MainLoop([0, 1000])
+    sc.MainLoop([0, 9000])
+    sc.ComputeMomentsMeta()
+    n = sc.GetDensityField()
+    u = sc._sim.get_velocity().reshape(2, 256, 256)
+    assert rel_err(n[128, :], z['row_10000']) <= TOL
+    assert rel_err(n[:, 128], z['col_10000']) <= TOL
+    assert rel_err(np.stack([u[0, 148, :], u[1, 148, :]], axis=1), z['urow_10000']) <= 1e-11
+    assert rel_err([n.max(), n.min()], [float(z['nmax_10000']), float(z['nmin_10000'])]) <= TOL
+    assert abs(n.sum() - float(z['nsum_10000'])) <= 1e-13 * float(z['nsum_10000'])
+    assert abs(np.abs(u).max() - float(z['umax_10000'])) <= 1e-11 * float(z['umax_10000'])
+    mass, _ = sc.MassMomentum()
+    assert abs(mass - float(z['mass_10000'])) <= 1e-13 * float(z['mass_10000'])
+    sc.End()
+
+
 def test_exact_literals_conserve_mass_1e13():
     """With exact coefficients the total mass is conserved to 1e-13 after 1000 steps
     (the reference's 15-digit literals drift by -8.4e-16 per step by design)."""
@@ -403,12 +428,14 @@ def test_density_readers_follow_the_single_pass_kernel():
 
 
 @pytest.mark.parametrize('st,dims', [('D3E6', (40, 24, 36)), ('D3E8', (32, 32, 24)), ('D3E6', (66, 18, 20)),
-                                     ('D3E6', (35, 16, 12))])
+                                     ('D3E6', (35, 16, 12)), ('D3E6', (4, 8, 6)), ('D3E8', (2, 16, 8))])
 @pytest.mark.parametrize('coll', ['bgk', 'mrt'])
 def test_single_pass_paired_halo_loads_bit_identical(st, dims, coll):
     """Paired halo loads (two x-adjacent cells per 8-byte load) sum in the same
     order as the scalar single pass, so the populations are bit-identical;
-    partial tiles in x and y, and an odd Lx (35: the scalar form runs)."""
+    partial tiles in x and y, an odd Lx (35: the scalar form runs), and boxes
+    narrower than the tile (Lx = 4 and 2), where a halo row wraps around the
+    box several times."""
     x, f = XIStencils['D3Q19'], FStencils[st]
     Q = 19
     rates = np.array([1.0, 1.0, 1.0] + [1.1 + 0.02 * i for i in range(Q - 3)])

@@ -52,7 +52,8 @@ def test_odd_width_would_straddle_the_wrap():
 
 
 def test_bgk_opposite_pair_split_equals_per_direction_form():
-    """The single pass makes a direction q and its opposite together from the
+    """A check of the algebra only (FP64 numpy, the kernel is not run): the
+    single pass makes a direction q and its opposite together from the
     even part t = a eu^2 + c eu eF and the odd part s = b eu + d eF of the
     factored BGK + Guo operator; in exact arithmetic (FP64 here) that equals
     the per-direction form w_q [C0 + eu (a eu + b + c eF) + d eF]."""

@@ -103,6 +103,35 @@ def test_step_noalloc_matches_handle_step(case):
     h.close()
 
 
+def test_step_noalloc_on_a_caller_stream():
+    """Two calls enqueued back to back on a stream the caller created, with no
+    host synchronisation between them: the second call's passes must run after
+    the first's (same stream), and both results equal the handle's steps."""
+    torch = pytest.importorskip('torch')
+    x, f = XIStencils['D3Q19'], FStencils['D3E6']
+    dims, Q = (24, 20, 16), 19
+    prm = _Params('D3Q19', 'D3E6', dims, -4.5, _lib.FP64)
+    h = _lib.Sim(3, dims, x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], -4.5)
+    h.set_tuning(_lib.PATH_TWO_PASS, 0)
+    h.set_density(droplet(dims, 5.0, 4.6, 0.2, 2.0, 9))
+    h.set_velocity(np.zeros(3 * h.V))
+    h.init_populations()
+    f0 = h.get_populations()
+    buf = [torch.from_numpy(f0).to('cuda'), torch.full((Q * h.V,), float('nan'), dtype=torch.float64, device='cuda')]
+    torch.cuda.synchronize()
+    s = torch.cuda.Stream()
+    handle = ctypes.c_void_p(s.cuda_stream)
+    for call in range(2):
+        _lib.call('sclbm_step_noalloc', ctypes.byref(prm.p), ctypes.c_void_p(buf[call % 2].data_ptr()),
+                  ctypes.c_void_p(buf[(call + 1) % 2].data_ptr()), handle)
+    s.synchronize()
+    h.step(2)
+    got = buf[0].cpu().numpy()
+    assert np.isfinite(got).all()
+    assert rel_err(got, h.get_populations()) <= 1e-12
+    h.close()
+
+
 def test_step_noalloc_rejects_lattices_beyond_its_scratch():
     torch = pytest.importorskip('torch')
     a = torch.empty(9 * 8, dtype=torch.float64, device='cuda')
