@@ -271,8 +271,9 @@ def stable_twin(dev, steps, ms_headline):
 
 def precision_table(dev, L=128, steps=5000):
     """FP32-shifted storage against the plain FP64 path on the 3D headline's
-    shape at the stable coupling: D3Q19 E6, MRT rates 1.0, droplet R = L*40/256,
-    G=-4.5, `steps` steps; errors of the density and velocity fields, of the
+    shape at the stable coupling: D3Q19 E6, MRT rates 1.0, a droplet of radius
+    L/4 (one of the headline's proportion, L*40/256, evaporates into the box at
+    this size), G=-4.5, `steps` steps; errors of the density and velocity fields, of the
     mass, of the Laplace pressure (PBulk of the centre and corner densities),
     and of the spurious-current magnitude max|u|.  Two FP32 shifts: the gas
     density (the library's choice for droplets) and the mean of the two
@@ -280,7 +281,7 @@ def precision_table(dev, L=128, steps=5000):
     from sclbm.profiles import droplet
     from sclbm.sweep import laplace_dp
     box = (L, L, L)
-    n0 = droplet(box, L * 40.0 / 256, RHO_L_STABLE, RHO_G_STABLE, WIDTH, SEED)
+    n0 = droplet(box, L / 4.0, RHO_L_STABLE, RHO_G_STABLE, WIDTH, SEED)
     V = n0.size
     c = L // 2
     probe = [c + L * c + L * L * c, V - 1]
@@ -303,7 +304,7 @@ def precision_table(dev, L=128, steps=5000):
                     umax=float(np.sqrt((u ** 2).sum(0)).max()), wall=wall)
 
     ref = run('fp64')
-    out = {'box': list(box), 'steps': steps, 'G': G_STABLE, 'R': L * 40.0 / 256,
+    out = {'box': list(box), 'steps': steps, 'G': G_STABLE, 'R': L / 4.0,
            'reference': 'plain FP64 GPU path (exact coefficients; within 1e-10 of the reference on the 2D twin)',
            'fp64': {'mass_drift': ref['mass_drift'], 'dp': ref['dp'], 'rho_in': ref['n_in'], 'rho_out': ref['n_out'],
                     'max_u': ref['umax'], 'wall_s': round(ref['wall'], 3)}}
@@ -352,7 +353,11 @@ def sweep_leg(dev, max_steps=100000, coex_steps=100000):
             'dp_rel_err_vs_fp64': {'median': float(np.median(errs)) if errs.size else None,
                                    'max': float(errs.max()) if errs.size else None,
                                    'within_1e-5': int((errs <= 1e-5).sum()), 'n': int(errs.size)},
-            'unstable': len(r['unstable'])}
+            'unstable': len(r['unstable']),
+            'not_converged_fp32': [{'R': int(b['radii'][j]), 'G': round(float(b['G'][j]), 4),
+                                    'steps': int(b['steps'][j]),
+                                    'fp64_steps': plain[j]['steps'] if plain[j] is not None else None}
+                                   for j in range(len(b['radii'])) if b['status'][j] == 'max_steps']}
 
 
 def profiled_traffic():

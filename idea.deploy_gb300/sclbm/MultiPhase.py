@@ -381,7 +381,9 @@ class ShanChenMultiPhase:
         self._simple_off()
         S = numeric_relaxation_matrix(relaxation_matrix, omega_syms_vals, self.sims_vars['Q'])
         key = ('mrt', S.tobytes())
-        if self._collision != key:
+        # explicit operator tables given at construction (collision_tables) are
+        # the operator to run, as in MainLoop
+        if self._collision != key and self._collision != ('tables',):
             self._sim.set_collision(_lib.COLL_MRT, mrt_s=S)
             self._collision = key
         return self._loop(time_steps, convergence_functions, profiling)
