@@ -437,6 +437,9 @@ def run_ours(a, dist):
     sim.set_density(n0)
     sim.set_velocity(np.zeros(3 * V))
     sim.init_populations()
+    # the autotuner picks the step variant (staging, tile shape, chunk) on
+    # this box: each candidate timed over trial steps that leave the state as it is
+    tuned, tuned_ms = sim.autotune(a.tune_steps) if a.tune_steps > 0 else (sim.get_tuning_ex(), None)
     sim.step(a.warmup)
     kps = sim.kernels_per_step()
     clocks = Clocks(dev)
@@ -470,6 +473,9 @@ def run_ours(a, dist):
         'step_path': {'path': 'single pass (k_fused, paired halo loads)' if path == 3 else
                       'single pass (k_fused)' if path == 2 else 'two passes (k_density_psi + k_fcs)',
                       'chunk_planes': chunk, 'grid': grid,
+                      'tuned': dict(tuned, trial_ms_per_step=tuned_ms,
+                                    tile_shape=['32x8', '64x8', '32x16', '128x8'][tuned.get('tile', 0)],
+                                    by='sclbm_autotune (%d trial launches per candidate)' % a.tune_steps),
                       'collision_kernel': 'MRT with all rates 1.0 is exactly BGK with omega=1: sparse BGK operator'},
         'roofline': {'bound': 'hbm', 'kernel': 'k_fused (single pass)' if path in (2, 3) else
                      'k_fcs (force+collide+push-stream pass)',
@@ -758,6 +764,7 @@ def main():
     ap.add_argument('--precision-box', type=int, default=128)
     ap.add_argument('--precision-steps', type=int, default=5000)
     ap.add_argument('--no-sweep', action='store_true', help='skip the bounded droplet-sweep leg')
+    ap.add_argument('--tune-steps', type=int, default=10, help='autotuner trial launches per candidate (0: off)')
     a = ap.parse_args()
     if a.box:
         global BOX

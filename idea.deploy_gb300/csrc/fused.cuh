@@ -35,12 +35,25 @@ namespace sclbm {
 //                   buffered, completed on an mbarrier, while plane m collides
 enum : int { STG_HALO_ASYNC = 1, STG_OWN_TMA = 2 };
 
-template <class L, class S>
+// Tile shapes of the 3D paired single pass (BGK): index 0 is the default
+// 32 x 8 (256 threads, four CTAs per SM); the others put wider rows (256 or
+// 512 bytes of a population row per CTA, which the memory system serves
+// better than 128-byte pieces) or more rows (a smaller halo share) in a CTA:
+// 64 x 8 and 32 x 16 (512 threads, two CTAs per SM), 128 x 8 (1024 threads,
+// one).  Every shape computes the same cells with the same arithmetic, so the
+// results are bit-identical; the autotuner picks among them.
+struct TileShape {
+    int tx, ty, minb;
+};
+constexpr TileShape kTiles[] = {{32, 8, 4}, {64, 8, 2}, {32, 16, 2}, {128, 8, 1}};
+constexpr int N_TILES = 4;
+
+template <class L, class S, int TXp = 0, int TYp = 0>
 struct FusedShape {
     static constexpr int D = L::D;
     static constexpr int R = S::R;
-    static constexpr int TX = D == 3 ? 32 : 256;     // tile width in x
-    static constexpr int TY = D == 3 ? 8 : 1;        // tile height in y (3D)
+    static constexpr int TX = TXp ? TXp : (D == 3 ? 32 : 256);  // tile width in x
+    static constexpr int TY = TYp ? TYp : (D == 3 ? 8 : 1);     // tile height in y (3D)
     static constexpr int NT = TX * TY;               // threads = interior cells per plane
     static constexpr int HX = TX + 2 * R;            // halo tile width
     static constexpr int HY = D == 3 ? TY + 2 * R : 1;
@@ -136,6 +149,7 @@ struct FusedGeom {
     int items;
     int pairs;  // 3D, even Lx and even halo radius: halo populations loaded two cells per load
     int stg;    // STG_* flags of the staged 3D variants (0: none)
+    int tile;   // index into kTiles (3D paired BGK; 0: the default shape)
     int *err;   // device flag set by a staged variant whose bounded wait gave up
 };
 
@@ -225,7 +239,8 @@ SCLBM_HD constexpr int opposite_e(int a) {
 // the caller passes the input's tensor map, the two mbarriers, the running
 // issue / wait counts of own-population boxes (k_issue-th box: buffer k & 1,
 // phase (k >> 1) & 1, the same on every thread) and the error flag.
-template <class L, class S, bool MRT, class ST = void, bool WALLS = false, bool PAIRS = false, int STG = 0>
+template <class L, class S, bool MRT, class ST = void, bool WALLS = false, bool PAIRS = false, int STG = 0,
+          int TXT = 0, int TYT = 0>
 __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float *__restrict__ pop_out, const int V,
                                            const int Lx, const int Ly, const int Lz, const int x0, const int y0,
                                            const int m0, const int m1, const float neg_g, const float rho0,
@@ -240,7 +255,7 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
     static_assert(STG == 0 || (PAIRS && !NOISE && !WALLS && L::D == 3), "staged variants: 3D paired halo loads");
     constexpr bool HALO_ASYNC = (STG & STG_HALO_ASYNC) != 0, OWN_TMA = (STG & STG_OWN_TMA) != 0;
     using SeedT = typename std::conditional<NOISE, ST, int>::type;
-    using SH = FusedShape<L, S>;
+    using SH = FusedShape<L, S, TXT, TYT>;
     constexpr int D = L::D, Q = L::Q, R = SH::R, HX = SH::HX, HC = SH::HC, NT = SH::NT, RING = SH::RING;
     float *ring = smem;  // psi ring [RING][HC], then (2D) 2 stage buffers [HPT][Q][NT]
     float *stage0 = smem + RING * HC;
@@ -572,11 +587,14 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
 // spills), BGK with one halo cell per load three (80 registers, no spills; 5%
 // faster than two at 256^3 D3Q19 E6, measured in one run), the dense MRT
 // operator two.
-template <class L, class S, bool MRT, bool PAIRS = false>
-__global__ void __launch_bounds__(FusedShape<L, S>::NT, MRT ? 2 : (PAIRS ? 4 : 3))
+// TILE (3D paired BGK only): index into kTiles; 0 keeps the default shape.
+template <class L, class S, bool MRT, bool PAIRS = false, int TILE = 0>
+__global__ void __launch_bounds__(TILE ? kTiles[TILE].tx * kTiles[TILE].ty : FusedShape<L, S>::NT,
+                                  TILE ? kTiles[TILE].minb : (MRT ? 2 : (PAIRS ? 4 : 3)))
     k_fused(const float *__restrict__ pop, float *__restrict__ pop_out, const __grid_constant__ StepParams<L, S, float> p,
             const FusedGeom fg) {
-    using SH = FusedShape<L, S>;
+    constexpr int TXT = TILE ? kTiles[TILE].tx : 0, TYT = TILE ? kTiles[TILE].ty : 0;
+    using SH = FusedShape<L, S, TXT, TYT>;
     constexpr int D = L::D;
     extern __shared__ float smem[];
     const int Lm = D == 3 ? fg.L[2] : fg.L[1];
@@ -586,8 +604,9 @@ __global__ void __launch_bounds__(FusedShape<L, S>::NT, MRT ? 2 : (PAIRS ? 4 : 3
         const int iy = D == 3 ? rest % fg.tiles_y : 0;
         const int ic = D == 3 ? rest / fg.tiles_y : rest;
         const int m0 = ic * fg.chunk;
-        fused_tile<L, S, MRT, void, false, PAIRS>(pop, pop_out, (int)fg.V, fg.L[0], fg.L[1], fg.L[2], ix * SH::TX,
-                                                  iy * SH::TY, m0, min(m0 + fg.chunk, Lm), p.neg_g, p.rho0, p, smem);
+        fused_tile<L, S, MRT, void, false, PAIRS, 0, TXT, TYT>(pop, pop_out, (int)fg.V, fg.L[0], fg.L[1], fg.L[2],
+                                                               ix * SH::TX, iy * SH::TY, m0, min(m0 + fg.chunk, Lm),
+                                                               p.neg_g, p.rho0, p, smem);
     }
 }
 

@@ -58,9 +58,9 @@ struct KernelOps {
     cudaError_t (*fused)(const void *pop, void *pop_out, const void *step_params, const FusedGeom &fg, int grid,
                          const void *tmap, cudaStream_t st);
     int fused_tx, fused_ty, fused_r;
-    int (*fused_occupancy)(int pairs, int stg);  // of the paired-load instance when pairs != 0
-    int fused_stg_mask;                          // STG_* variants built for this kernel set (0: none)
-    int (*fused_smem)(int pairs, int stg);       // dynamic shared memory of a launch
+    int (*fused_occupancy)(int pairs, int stg, int tile);  // of the paired-load instance when pairs != 0
+    int fused_stg_mask;  // STG_* variants built for this kernel set (0: none)
+    int fused_tile_mask; // kTiles shapes built (bit t) for the paired single pass (bit 0: the default)
     // batches of lattices (FP32 only, else null)
     cudaError_t (*batch_step)(const void *pop, void *pop_out, const void *sp, const BatchInst *inst, const int4 *items,
                               int n_items, int Vtot, int *counter, int parity, int pairs, int grid, cudaStream_t st);
@@ -195,10 +195,35 @@ struct Ops {
     // staged variants: 3D, even radius, BGK, FP32
     static constexpr bool STG_BUILT = std::is_same<Real, float>::value && L::D == 3 && S::R % 2 == 0 && !MRT;
     static constexpr int STG_MASK = STG_BUILT ? 3 : 0;
-    static int fused_smem(int pairs, int stg) {
-        using SH = FusedShape<L, S>;
-        if (pairs && stg) return SH::stg_smem(stg) + 128;
-        return SH::SMEM;
+    static constexpr int TILE_MASK = STG_BUILT ? (1 << N_TILES) - 1 : 1;
+    template <int TILE>
+    static void allow_tile_smem() {
+        using SH = FusedShape<L, S, kTiles[TILE].tx, kTiles[TILE].ty>;
+        static bool done[64] = {};
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (dev < 0 || dev >= 64 || !done[dev]) {
+            cudaFuncSetAttribute(k_fused<L, S, MRT, true, TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 SH::SMEM);
+            if (dev >= 0 && dev < 64) done[dev] = true;
+        }
+    }
+    template <int TILE>
+    static cudaError_t launch_tile(const void *pop, void *pop_out, const void *sp, const FusedGeom &fg, int grid,
+                                   cudaStream_t st) {
+        using SH = FusedShape<L, S, kTiles[TILE].tx, kTiles[TILE].ty>;
+        allow_tile_smem<TILE>();
+        k_fused<L, S, MRT, true, TILE><<<grid, SH::NT, SH::SMEM, st>>>((const float *)pop, (float *)pop_out,
+                                                                      *static_cast<const SP *>(sp), fg);
+        return cudaGetLastError();
+    }
+    template <int TILE>
+    static int occupancy_tile() {
+        using SH = FusedShape<L, S, kTiles[TILE].tx, kTiles[TILE].ty>;
+        allow_tile_smem<TILE>();
+        int b = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fused<L, S, MRT, true, TILE>, SH::NT, SH::SMEM);
+        return b > 0 ? b : 1;
     }
     template <int STG>
     static cudaError_t launch_stg(const void *pop, void *pop_out, const void *sp, const FusedGeom &fg, int grid,
@@ -229,8 +254,11 @@ struct Ops {
                 if (fg.pairs && fg.stg == 1) return launch_stg<1>(pop, pop_out, sp, fg, grid, tmap, st);
                 if (fg.pairs && fg.stg == 2) return launch_stg<2>(pop, pop_out, sp, fg, grid, tmap, st);
                 if (fg.pairs && fg.stg == 3) return launch_stg<3>(pop, pop_out, sp, fg, grid, tmap, st);
+                if (fg.pairs && !fg.stg && fg.tile == 1) return launch_tile<1>(pop, pop_out, sp, fg, grid, st);
+                if (fg.pairs && !fg.stg && fg.tile == 2) return launch_tile<2>(pop, pop_out, sp, fg, grid, st);
+                if (fg.pairs && !fg.stg && fg.tile == 3) return launch_tile<3>(pop, pop_out, sp, fg, grid, st);
             }
-            if (fg.stg) return cudaErrorNotSupported;
+            if (fg.stg || fg.tile) return cudaErrorNotSupported;
             if constexpr (L::D == 3 && S::R % 2 == 0) {
                 if (fg.pairs) {
                     k_fused<L, S, MRT, true><<<grid, SH::NT, SH::SMEM, st>>>((const float *)pop, (float *)pop_out,
@@ -269,7 +297,7 @@ struct Ops {
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fused_stg<L, S, MRT, STG>, SH::NT, SH::stg_smem(STG) + 128);
         return b > 0 ? b : 1;
     }
-    static int fused_occupancy(int pairs, int stg) {
+    static int fused_occupancy(int pairs, int stg, int tile) {
         if constexpr (std::is_same<Real, float>::value) {
             using SH = FusedShape<L, S>;
             allow_smem();
@@ -277,6 +305,9 @@ struct Ops {
                 if (pairs && stg == 1) return occupancy_stg<1>();
                 if (pairs && stg == 2) return occupancy_stg<2>();
                 if (pairs && stg == 3) return occupancy_stg<3>();
+                if (pairs && tile == 1) return occupancy_tile<1>();
+                if (pairs && tile == 2) return occupancy_tile<2>();
+                if (pairs && tile == 3) return occupancy_tile<3>();
             }
             int b = 0;
             if constexpr (L::D == 3 && S::R % 2 == 0) {
@@ -547,7 +578,7 @@ struct Ops {
         static const KernelOps o = {sizeof(SP), sizeof(EP), f32 ? 1 : 2, &fill_step, &fill_eq, &density,
                                     &fcs, &velocity, &density_walls, &fcs_walls, &init_pop, &grids,
                                     f32 ? &fused : nullptr, SH::TX, SH::TY, SH::R,
-                                    f32 ? &fused_occupancy : nullptr, STG_MASK, &fused_smem,
+                                    f32 ? &fused_occupancy : nullptr, STG_MASK, TILE_MASK,
                                     f32 ? &batch_step : nullptr, f32 ? &batch_density : nullptr,
                                     f32 ? &batch_moments : nullptr, f32 ? &batch_mass : nullptr,
                                     f32 ? &batch_add_rest : nullptr, f32 ? &batch_probe : nullptr,

@@ -255,6 +255,7 @@ struct sclbm_sim {
     FusedGeom fg = {};
     int fused_grid = 0, path = SCLBM_PATH_AUTO, chunk_override = 0;
     int staging = -1;  // requested SCLBM_STAGE_* flags of the 3D single pass (-1: automatic)
+    int tile = -1;     // requested tile shape (index into kTiles) of the 3D paired single pass (-1: automatic)
     // tensor maps of the two population buffers (4D: x, y, plane, q; box of one
     // tile plane), encoded when a staged variant with TMA loads is planned
     CUtensorMap tmap[2];
@@ -551,14 +552,16 @@ void plan_fused(sclbm_sim *s) {
     if (!o->fused) return;
     sclbm_tuning tuned;
     if (s->path == SCLBM_PATH_AUTO && s->chunk_override == 0 && s->staging < 0 && cached_tuning(s, &tuned)) {
-        const int saved_path = s->path, saved_chunk = s->chunk_override, saved_stg = s->staging;
+        const int saved_path = s->path, saved_chunk = s->chunk_override, saved_stg = s->staging, saved_tile = s->tile;
         s->path = tuned.path == SCLBM_PATH_FUSED ? SCLBM_PATH_FUSED : SCLBM_PATH_AUTO;
         s->chunk_override = tuned.chunk;
         s->staging = tuned.staging;
+        s->tile = tuned.tile;
         plan_fused(s);
         s->path = saved_path;
         s->chunk_override = saved_chunk;
         s->staging = saved_stg;
+        s->tile = saved_tile;
         return;
     }
     FusedGeom &g = s->fg;
@@ -573,9 +576,18 @@ void plan_fused(sclbm_sim *s) {
               o->fused_r % 2 == 0;
     g.stg = plan_staging(s, g.pairs);
     g.err = s->flag_dev;
+    // another tile shape (3D paired BGK, not staged, no walls or noise)
+    g.tile = 0;
+    if (g.pairs && !g.stg && !s->walls && !s->noise_kind && s->tile > 0 && s->tile < N_TILES &&
+        (o->fused_tile_mask >> s->tile & 1))
+        g.tile = s->tile;
+    if (g.tile) {
+        g.tiles_x = (s->L[0] + kTiles[g.tile].tx - 1) / kTiles[g.tile].tx;
+        g.tiles_y = (s->L[1] + kTiles[g.tile].ty - 1) / kTiles[g.tile].ty;
+    }
     const int resident = s->sms * (s->noise_kind ? o->fused_noise_occupancy()
                                    : s->walls    ? o->fused_walls_occupancy()
-                                                 : o->fused_occupancy(g.pairs, g.stg));
+                                                 : o->fused_occupancy(g.pairs, g.stg, g.tile));
     const int base = g.tiles_x * g.tiles_y;
     int best_c = 1;
     double best = -1;
@@ -1286,10 +1298,15 @@ int sclbm_set_tuning_ex(sclbm_sim *s, const sclbm_tuning *t) {
     if (!s || !t) return fail(SCLBM_ERR_ARG, "null argument");
     if (t->staging < -1 || t->staging > (SCLBM_STAGE_HALO_ASYNC | SCLBM_STAGE_OWN_TMA))
         return fail(SCLBM_ERR_ARG, "staging %d", t->staging);
-    const int saved = s->staging;
+    if (t->tile < -1 || t->tile >= N_TILES) return fail(SCLBM_ERR_ARG, "tile %d (0 .. %d)", t->tile, N_TILES - 1);
+    const int saved = s->staging, saved_tile = s->tile;
     s->staging = t->staging;
+    s->tile = t->tile;
     const int rc = sclbm_set_tuning(s, t->path, t->chunk);
-    if (rc) s->staging = saved;
+    if (rc) {
+        s->staging = saved;
+        s->tile = saved_tile;
+    }
     return rc;
 }
 
@@ -1297,6 +1314,7 @@ int sclbm_get_tuning_ex(const sclbm_sim *s, sclbm_tuning *t) {
     if (!s || !t) return fail(SCLBM_ERR_ARG, "null argument");
     sclbm_get_tuning(s, &t->path, &t->chunk, &t->grid);
     t->staging = fused_path(s) ? s->fg.stg : 0;
+    t->tile = fused_path(s) ? s->fg.tile : 0;
     return SCLBM_OK;
 }
 
@@ -1321,13 +1339,13 @@ int sclbm_autotune(sclbm_sim *s, int trial_steps, sclbm_tuning *best, double *be
                                            "write the current populations)");
     DevGuard dg(s->device);
     CUDA_TRY(cudaStreamSynchronize(s->st));
-    const int saved_path = s->path, saved_chunk = s->chunk_override, saved_stg = s->staging;
+    const int saved_path = s->path, saved_chunk = s->chunk_override, saved_stg = s->staging, saved_tile = s->tile;
     struct Cand {
-        int path, chunk, staging;
+        int path, chunk, staging, tile;
     };
     std::vector<Cand> cands;
     if (!fused_path(s)) {
-        cands.push_back({s->path, 0, 0});
+        cands.push_back({s->path, 0, 0, 0});
     } else {
         const int Lm = s->D == 3 ? s->L[2] : s->L[1];
         const bool pairs_ok = s->D == 3 && s->L[0] % 2 == 0 && s->ops->fused_r % 2 == 0 && !s->walls;
@@ -1336,26 +1354,33 @@ int sclbm_autotune(sclbm_sim *s, int trial_steps, sclbm_tuning *best, double *be
             if (c < Lm) chunks.push_back(c);
         std::vector<int> paths = {SCLBM_PATH_FUSED};
         if (pairs_ok) paths.insert(paths.begin(), SCLBM_PATH_FUSED_PAIRS);
-        for (int path : paths)
+        for (int path : paths) {
             for (int stg = 0; stg <= 3; stg++) {
                 if (stg && (path != SCLBM_PATH_FUSED_PAIRS || !(s->ops->fused_stg_mask & stg))) continue;
-                for (int c : chunks) cands.push_back({path, c, stg});
+                for (int c : chunks) cands.push_back({path, c, stg, 0});
             }
+            if (path == SCLBM_PATH_FUSED_PAIRS)
+                for (int tile = 1; tile < N_TILES; tile++)
+                    if (s->ops->fused_tile_mask >> tile & 1)
+                        for (int c : chunks) cands.push_back({path, c, 0, tile});
+        }
     }
     cudaEvent_t e0, e1;
     CUDA_TRY(cudaEventCreate(&e0));
     CUDA_TRY(cudaEventCreate(&e1));
     double best_t = 1e300;
     Cand win = cands[0];
-    std::vector<std::array<int, 4>> seen;  // effective (pairs, staging, chunk, grid) already timed
+    std::vector<std::array<int, 5>> seen;  // effective (pairs, staging, tile, chunk, grid) already timed
     int rc = SCLBM_OK;
     for (const Cand &c : cands) {
         s->path = c.path;
         s->chunk_override = c.chunk;
         s->staging = c.staging;
+        s->tile = c.tile;
         plan_fused(s);
-        const std::array<int, 4> eff = {fused_path(s) ? s->fg.pairs : -1, fused_path(s) ? s->fg.stg : -1,
-                                        fused_path(s) ? s->fg.chunk : 0, fused_path(s) ? s->fused_grid : 0};
+        const bool fp = fused_path(s);
+        const std::array<int, 5> eff = {fp ? s->fg.pairs : -1, fp ? s->fg.stg : -1, fp ? s->fg.tile : -1,
+                                        fp ? s->fg.chunk : 0, fp ? s->fused_grid : 0};
         if (std::find(seen.begin(), seen.end(), eff) != seen.end()) continue;
         seen.push_back(eff);
         // one untimed launch, then trial_steps timed ones, all from the current buffer
@@ -1383,12 +1408,14 @@ int sclbm_autotune(sclbm_sim *s, int trial_steps, sclbm_tuning *best, double *be
         s->path = saved_path;
         s->chunk_override = saved_chunk;
         s->staging = saved_stg;
+        s->tile = saved_tile;
         plan_fused(s);
         return rc;
     }
     s->path = win.path;
     s->chunk_override = win.chunk;
     s->staging = win.staging;
+    s->tile = win.tile;
     plan_fused(s);
     for (auto &g : s->graph)
         if (g) cudaGraphExecDestroy(g), g = nullptr;
@@ -1857,7 +1884,7 @@ void batch_items(const sclbm_batch *b, int chunk, std::vector<int4> &items) {
 }
 
 int batch_plan(sclbm_batch *b) {
-    const int resident = b->sms * b->ops->fused_occupancy(0, 0);
+    const int resident = b->sms * b->ops->fused_occupancy(0, 0, 0);
     int chunk = BATCH_CHUNK;
     std::vector<int4> items;
     batch_items(b, chunk, items);
