@@ -160,22 +160,36 @@ __global__ void __launch_bounds__(BATCH_THREADS) k_batch_add_rest(float *__restr
 // (K_NInNOut, idpy/LBM/LBMKernels.py:506-523).  One warp per lattice.
 template <class L>
 __global__ void __launch_bounds__(32) k_batch_probe(const float *__restrict__ pop, const BatchInst *__restrict__ inst,
-                                                   const int Vtot, double *out) {
+                                                   const int Vtot, double *out, const int rad) {
+    // density at the centre cell and at the last cell (DeltaPLaplace's two
+    // probes), each the FP64 mean over the cube of side 2 rad + 1 about the
+    // cell (periodic); rad = 0 is the single cell.  One warp per lattice,
+    // cells taken in a fixed order by fixed lanes (reproducible sums).
     const BatchInst I = inst[blockIdx.x];
     if (!I.active) return;
-    const int V = I.Lx * I.Ly * I.Lz;
-    const int c = I.Lx / 2 + I.Lx * (I.Ly / 2 + I.Ly * (L::D == 3 ? I.Lz / 2 : 0));
-    const int q = threadIdx.x;
-    double a = q < L::Q ? (double)pop[q * Vtot + I.base + c] : 0.0;
-    double b = q < L::Q ? (double)pop[q * Vtot + I.base + V - 1] : 0.0;
+    constexpr int D = L::D;
+    const int side = 2 * rad + 1, cells = D == 3 ? side * side * side : side * side;
+    const int Ls[3] = {I.Lx, I.Ly, D == 3 ? I.Lz : 1};
+    const int cen[2][3] = {{I.Lx / 2, I.Ly / 2, D == 3 ? I.Lz / 2 : 0}, {I.Lx - 1, I.Ly - 1, D == 3 ? I.Lz - 1 : 0}};
+    for (int which = 0; which < 2; which++) {
+        double acc = 0.0;
+        for (int t = threadIdx.x; t < cells; t += 32) {
+            int o[3] = {t % side - rad, (t / side) % side - rad, D == 3 ? t / (side * side) - rad : 0};
+            int idx = 0, stride = 1;
+            for (int d = 0; d < 3; d++) {
+                int v = (cen[which][d] + o[d]) % Ls[d];
+                if (v < 0) v += Ls[d];
+                idx += v * stride;
+                stride *= Ls[d];
+            }
+            double n = 0.0;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        a += __shfl_down_sync(0xffffffffu, a, o);
-        b += __shfl_down_sync(0xffffffffu, b, o);
-    }
-    if (q == 0) {
-        out[2 * blockIdx.x] = (double)I.rho0 + a;
-        out[2 * blockIdx.x + 1] = (double)I.rho0 + b;
+            for (int q = 0; q < L::Q; q++) n += (double)pop[(int64_t)q * Vtot + I.base + idx];
+            acc += n;
+        }
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+        if (threadIdx.x == 0) out[2 * blockIdx.x + which] = (double)I.rho0 + acc / cells;
     }
 }
 

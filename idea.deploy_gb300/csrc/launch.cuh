@@ -73,7 +73,7 @@ struct KernelOps {
                               cudaStream_t st);
     cudaError_t (*batch_add_rest)(void *pop, const BatchInst *inst, int n_inst, const float *delta, int gx,
                                   cudaStream_t st);
-    cudaError_t (*batch_probe)(const void *pop, const BatchInst *inst, int n_inst, int Vtot, double *out,
+    cudaError_t (*batch_probe)(const void *pop, const BatchInst *inst, int n_inst, int Vtot, double *out, int rad,
                                cudaStream_t st);
     // fluctuating step (BGK only, else null): parameter block, its filler from the
     // noise operator (m2var[nr], coef[q*nr]) and the launcher; grid from occupancy
@@ -387,10 +387,10 @@ struct Ops {
         }
         return cudaErrorNotSupported;
     }
-    static cudaError_t batch_probe(const void *pop, const BatchInst *inst, int n_inst, int Vtot, double *out,
+    static cudaError_t batch_probe(const void *pop, const BatchInst *inst, int n_inst, int Vtot, double *out, int rad,
                                    cudaStream_t st) {
         if constexpr (std::is_same<Real, float>::value) {
-            k_batch_probe<L><<<n_inst, 32, 0, st>>>((const float *)pop, inst, Vtot, out);
+            k_batch_probe<L><<<n_inst, 32, 0, st>>>((const float *)pop, inst, Vtot, out, rad);
             return cudaGetLastError();
         }
         return cudaErrorNotSupported;

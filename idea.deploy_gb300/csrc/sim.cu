@@ -1820,6 +1820,7 @@ struct sclbm_batch {
     void *dn = nullptr, *psi = nullptr, *u_old = nullptr;
     double *partials = nullptr;
     double *probe_d = nullptr;  // [2n] centre / last-cell densities
+    int probe_rad = 0;          // probes average the cube of side 2 rad + 1 about each cell
     float *delta_d = nullptr;   // [n] rest-population corrections
     int gx = 1, grid = 1, chunk = 32;
     int pairs = 0;          // 3D, even radius, every Lx and first cell even: paired halo loads
@@ -2283,11 +2284,19 @@ int sclbm_batch_restore_mass(sclbm_batch *b, const double *target, double *befor
     return SCLBM_OK;
 }
 
+int sclbm_batch_set_probe_radius(sclbm_batch *b, int rad) {
+    if (!b) return fail(SCLBM_ERR_ARG, "null handle");
+    if (rad < 0 || rad > 4) return fail(SCLBM_ERR_ARG, "probe radius %d (0 .. 4)", rad);
+    b->probe_rad = rad;
+    return SCLBM_OK;
+}
+
 int sclbm_batch_probe(sclbm_batch *b, double *n_in, double *n_out) {
     if (!b) return fail(SCLBM_ERR_ARG, "null handle");
     if (!b->pop_set) return fail(SCLBM_ERR_STATE, "populations are not initialized");
     DevGuard dg(b->device);
-    cudaError_t e = b->ops->batch_probe(b->pop[b->cur], b->inst_d, b->n, (int)b->Vtot, b->probe_d, b->st);
+    cudaError_t e = b->ops->batch_probe(b->pop[b->cur], b->inst_d, b->n, (int)b->Vtot, b->probe_d, b->probe_rad,
+                                        b->st);
     if (e != cudaSuccess) return fail(SCLBM_ERR_CUDA, "batch probe: %s", cudaGetErrorString(e));
     std::vector<double> v((size_t)2 * b->n);
     CUDA_TRY(cudaMemcpyAsync(v.data(), b->probe_d, v.size() * sizeof(double), cudaMemcpyDeviceToHost, b->st));

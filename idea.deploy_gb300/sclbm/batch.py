@@ -112,6 +112,10 @@ class Batch:
         _lib.call('sclbm_batch_restore_mass', self.h, _lib.ptr(t), _lib.ptr(before))
         return before
 
+    def set_probe_radius(self, rad):
+        """probe() returns means over the cube of side 2 rad + 1 about each cell."""
+        _lib.call('sclbm_batch_set_probe_radius', self.h, int(rad))
+
     def probe(self):
         """Per-lattice density at the centre cell and at the last cell."""
         a, b = np.full(self.n, np.nan), np.full(self.n, np.nan)

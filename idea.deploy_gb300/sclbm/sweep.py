@@ -119,7 +119,7 @@ def sweep_geometry(radii, multiple=32, factor=4):
 
 def ragged_sweep(radii, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, check_every=500, tol_dp=2e-5,
                  patience=4, max_steps=200000, noise=0.0, seed=0, device=0, init=None, mass_fix=True,
-                 residual_steps=100, residual_max=None, return_fields=False, dim=2, boxes=None):
+                 residual_steps=100, residual_max=None, return_fields=False, dim=2, boxes=None, probe_rad=None):
     """Run all droplets in one FP32 batch until each converges; returns a dict
     of per-droplet arrays and the wall time.  ``init`` may give initial
     density fields (e.g. a learned warm start) instead of the tanh profile,
@@ -143,6 +143,10 @@ def ragged_sweep(radii, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, che
     for i in range(n):
         b.set_density(i, init[i] if init is not None else cold(i))
     b.init_populations()
+    # the Laplace-pressure probes average a small bulk block (5x5 in 2D, 3x3x3
+    # in 3D): a single FP32 cell's rounding noise is a few 1e-5 of a large
+    # droplet's Laplace pressure, above the criterion's 2e-5
+    b.set_probe_radius((2 if dim == 2 else 1) if probe_rad is None else probe_rad)
     residual = np.full(n, np.nan)
     fallback = np.zeros(n, bool)
     if init is not None and residual_max is not None:
@@ -262,12 +266,28 @@ def laplace_fit(G=-4.5, radii=(12, 16, 20, 24, 32, 40, 48), stencil='D2E8', devi
     th = thermo.coexistence(G, f['Es'], f['Ws'])
     radii = list(radii)
     r = ragged_sweep(radii, [G] * len(radii), [th['n_l']] * len(radii), [th['n_g']] * len(radii),
-                     stencil=stencil, device=device, **kw)
+                     stencil=stencil, device=device, return_fields=True, **kw)
     ok = r['status'] == 'converged'
-    A = np.stack([1.0 / r['radii'][ok], np.ones(ok.sum())], 1)
-    (sigma, c), *_ = np.linalg.lstsq(A, r['dp'][ok], rcond=None)
-    return dict(G=G, sigma=float(sigma), intercept=float(c), sigma_thermo=th['sigma_f'],
-                radii=[int(v) for v in r['radii']], dp=[float(v) for v in r['dp']],
+    # equimolar radius of each equilibrated droplet: the area the liquid would
+    # fill at the measured inside / outside densities, A = (M - n_out V) / (n_in - n_out)
+    req = []
+    for j, fld in enumerate(r['fields']):
+        A = (fld.sum() - r['n_out'][j] * fld.size) / (r['n_in'][j] - r['n_out'][j])
+        req.append(math.sqrt(max(A, 0.0) / math.pi))
+    req = np.array(req)
+
+    def fit(R):
+        M = np.stack([1.0 / R[ok], np.ones(ok.sum())], 1)
+        (sg, c), *_ = np.linalg.lstsq(M, r['dp'][ok], rcond=None)
+        return float(sg), float(c)
+
+    sigma, c = fit(r['radii'].astype(float))
+    sigma_eq, c_eq = fit(req)
+    return dict(G=G, sigma=sigma, intercept=c, sigma_equimolar=sigma_eq, intercept_equimolar=c_eq,
+                sigma_thermo=th['sigma_f'], radii=[int(v) for v in r['radii']],
+                radii_equimolar=[float(v) for v in req], dp=[float(v) for v in r['dp']],
+                n_in=[float(v) for v in r['n_in']], n_out=[float(v) for v in r['n_out']],
+                rho_l_thermo=th['n_l'], rho_g_thermo=th['n_g'],
                 status=[str(v) for v in r['status']], steps=[int(v) for v in r['steps']])
 
 

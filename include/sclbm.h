@@ -375,6 +375,13 @@ SCLBM_API int sclbm_batch_restore_mass(sclbm_batch *b, const double *target, dou
  * of DeltaPLaplace (idpy/LBM/MultiPhase.py:1690-1757, K_NInNOut
  * idpy/LBM/LBMKernels.py:506-523).  Retired lattices keep their last values. */
 SCLBM_API int sclbm_batch_probe(sclbm_batch *b, double *n_in, double *n_out);
+/* make sclbm_batch_probe return the mean density over the cube (square in 2D)
+ * of side 2 rad + 1 about each probe cell, rad in [0, 4] (0, the default: the
+ * single cell).  For FP32-shifted storage: the rounding noise of one cell's
+ * stored populations (~1e-7 of the liquid density) is a few 1e-5 of the Laplace
+ * pressure of a large droplet; the mean over 25 or 27 bulk cells, which agree
+ * in equilibrium, lowers it about five-fold.  No counterpart in the reference. */
+SCLBM_API int sclbm_batch_set_probe_radius(sclbm_batch *b, int rad);
 
 /* ---------------------------------------------------------------------------
  * Warm-start surrogate: an MLP 5 -> 64 -> 64 -> 64 -> 1 with SiLU, BF16

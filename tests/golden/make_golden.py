@@ -99,6 +99,13 @@ FULL_TWIN = dict(xi='D2Q9', fs='D2E4', tau=1.0, G=-4.5, psi='exp', dims=(256, 25
 CFG2_64 = dict(xi='D3Q19', fs='D3E6', tau=1.0, G=-4.5, psi='exp', dims=(64, 64, 64),
                R=16.0, rl=4.636, rg=0.147, width=2.0, steps=[100, 1000], rates=[1.0] * 19)
 
+# A flat-interface (slab) run of the reference at a coupling where it settles:
+# D2Q9, E4, G = -4.5, tau = 1, a 64 x 4 periodic box with a liquid slab of
+# width 32 from the reference's own InitFlatInterface (n_g = 0.2, n_l = 4.55);
+# the run reaches u_conv < 1e-12 by about 70,000 steps.
+FLAT_E4 = dict(xi='D2Q9', fs='D2E4', tau=1.0, G=-4.5, psi='exp', dims=(64, 4), n_g=0.2, n_l=4.55, width=32.0,
+               steps=[10000, 40000, 70000])
+
 SEED = 1234
 
 
@@ -350,6 +357,36 @@ def gen_cfg2_64():
     print('cfg2_64 done in %.1f s' % (time.time() - t0), flush=True)
 
 
+def gen_flat_e4():
+    c = FLAT_E4
+    t0 = time.time()
+    sc = make_sim(c)
+    with contextlib.redirect_stdout(io.StringIO()):
+        sc.InitFlatInterface(n_g=c['n_g'], n_l=c['n_l'], width=c['width'], direction=0)
+    rec = {'n_init': sc.GetDensityField().copy()}
+    steps = list(c['steps'])
+    state = dict(k=0)
+    from idpy.LBM.MultiPhaseLoopChecks import CheckUConvergenceSCMP
+
+    def recorder(lbm):
+        k = steps[state['k']]
+        state['k'] += 1
+        lbm.ComputeMomentsMeta()
+        n = lbm.GetDensityField()
+        rec['n_%d' % k] = n.copy()
+        rec['umax_%d' % k] = float(np.abs(lbm.sims_idpy_memory['u'].D2H()).max())
+        with contextlib.redirect_stdout(io.StringIO()):
+            CheckUConvergenceSCMP(lbm)
+        rec['uconv_%d' % k] = float(lbm.sims_vars['u_conv'][-1])
+        return False
+
+    with contextlib.redirect_stdout(io.StringIO()):
+        sc.MainLoop([0] + steps, convergence_functions=[recorder])
+    np.savez_compressed(os.path.join(HERE, 'flat_e4_g45.npz'), **rec,
+                        config_json=np.array(json.dumps(c)))
+    print('flat_e4_g45 done in %.1f s' % (time.time() - t0), flush=True)
+
+
 def gen_init_profiles():
     """The reference's own interface-initialisation kernels (width 1)."""
     rec = {}
@@ -409,7 +446,8 @@ def main():
     ap.add_argument('cases', nargs='*')
     a = ap.parse_args()
     setup_reference(os.path.abspath(a.reference))
-    todo = a.cases or (list(CASES) + ['div_cfg1', 'full_twin_256', 'cfg2_64', 'init_profiles', 'mrt_basis'])
+    todo = a.cases or (list(CASES) + ['div_cfg1', 'full_twin_256', 'cfg2_64', 'flat_e4_g45', 'init_profiles',
+                                       'mrt_basis'])
     for name in todo:
         if name in CASES:
             gen_case(name, CASES[name])
@@ -419,6 +457,8 @@ def main():
             gen_full_twin()
         elif name == 'cfg2_64':
             gen_cfg2_64()
+        elif name == 'flat_e4_g45':
+            gen_flat_e4()
         elif name == 'init_profiles':
             gen_init_profiles()
         elif name == 'mrt_basis':

@@ -116,6 +116,28 @@ def test_batch_probe_reads_centre_and_last_cell():
     b.close()
 
 
+def test_batch_probe_block_means():
+    """With a probe radius the probes are FP64 means over the (2 rad + 1)^D
+    block about the centre cell and about the last cell (periodic)."""
+    lat, st, dims, G, rho0 = CASES['2d']
+    n0 = densities(dims)
+    b = Batch(XIStencils[lat], FStencils[st], dims, G, rho0)
+    for i, n in enumerate(n0):
+        b.set_density(i, n)
+    b.init_populations()
+    b.step(11)
+    b.set_probe_radius(2)
+    ni, no = b.probe()
+    for i, d in enumerate(dims):
+        nf = b.get_density(i)
+        cy, cx = d[1] // 2, d[0] // 2
+        blk = nf[cy - 2:cy + 3, cx - 2:cx + 3]
+        corner = np.roll(np.roll(nf, 2, axis=0), 2, axis=1)[-5:, -5:]   # rows/cols L-3 .. L+1 (periodic)
+        assert abs(ni[i] - blk.mean()) < 1e-12 * abs(ni[i])
+        assert abs(no[i] - corner.mean()) < 1e-12 * abs(no[i])
+    b.close()
+
+
 def test_batch_restore_mass_sets_each_lattice_mass():
     lat, st, dims, G, rho0 = CASES['2d']
     n0 = densities(dims)
