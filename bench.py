@@ -678,7 +678,8 @@ def run_warmstart_mode(a):
     train_set, test_set = warmstart.split(prof, holdout=512)
     m, loss, wall_train = warmstart.train(train_set, steps=a.ws_train_steps, batch=8192, lr=1e-3)
     ev = warmstart.evaluate(m, test_set)
-    r = sweep.run_sweep(n=a.sweep_n, max_steps=a.sweep_max_steps, plain=not a.no_plain, mlp=m)
+    r = sweep.run_sweep(n=a.sweep_n, max_steps=a.sweep_max_steps, plain=not a.no_plain, mlp=m,
+                        plain_stop_at_dp=True)
     plain = r.get('plain')
     out = {'metric': 'D2Q9 E8 droplet sweep with a learned warm start: time to converge', 'unit': 's',
            'profiles': {'requested': a.ws_profiles, 'status': st['status'], 'wall_s': round(st['wall_s'], 2),
@@ -698,6 +699,53 @@ def run_warmstart_mode(a):
                                                  for k in ('converged', 'max_steps', 'diverged')}}
         out['speedup_wall_cold'] = round(r['plain_wall_s'] / r['batch']['wall_s'], 2)
         out['speedup_wall_warm'] = round(r['plain_wall_s'] / r['warm']['wall_s'], 2)
+    out['total_wall_s'] = round(time.perf_counter() - t0, 1)
+    m.close()
+    return out
+
+
+def run_warmstart3d_mode(a):
+    """Learned warm start in 3D (cfg 5): plain-method 3D equilibrium profiles
+    (D3Q19 E6 droplets in 96^3 boxes), the MLP trained on them on the device,
+    then the 256-droplet 3D sweep run cold and warm (cold-start fallback above
+    the residual threshold) against the plain FP64 path on a timed sample, all
+    arms stopped by the same Laplace-pressure criterion."""
+    from sclbm import sweep, warmstart
+    t0 = time.perf_counter()
+    prof, st = warmstart.equilibrium_profiles_3d(n=a.ws3d_profiles, seed=11, L=96)
+    train_set, test_set = warmstart.split(prof, holdout=max(8, a.ws3d_profiles // 8))
+    m, loss, wall_train = warmstart.train(train_set, steps=a.ws_train_steps, batch=8192, lr=1e-3)
+    ev = warmstart.evaluate(m, test_set)
+    r = sweep.run_sweep3d(n=a.sweep3d_n, max_steps=a.sweep3d_max_steps, plain_sample=a.sweep3d_plain, mlp=m,
+                          residual_max=0.1, plain_stop_at_dp=True)
+    b, w = r['batch'], r['warm']
+    ok = (b['status'] == 'converged') & (w['status'] == 'converged')
+    out = {'metric': 'D3Q19 E6 droplets (96^3) with a learned warm start: time to converge', 'unit': 's',
+           'profiles': {'requested': a.ws3d_profiles, 'status': st['status'], 'wall_s': round(st['wall_s'], 2),
+                        'train': len(train_set), 'held_out': len(test_set)},
+           'training': {'steps': a.ws_train_steps, 'wall_s': round(wall_train, 3),
+                        'loss_first': float(loss[:10].mean()), 'loss_last': float(loss[-100:].mean())},
+           'held_out': ev, 'config': r['config'],
+           'batch_cold': {'wall_s': round(b['wall_s'], 2),
+                          'status': {str(k): int((b['status'] == k).sum()) for k in set(b['status'])},
+                          'steps_mean_converged': float(b['steps'][b['status'] == 'converged'].mean())},
+           'batch_warm': {'wall_s': round(w['wall_s'], 2),
+                          'status': {str(k): int((w['status'] == k).sum()) for k in set(w['status'])},
+                          'steps_mean_converged': float(w['steps'][w['status'] == 'converged'].mean()),
+                          'cold_fallbacks': int(w['fallback'].sum()),
+                          'residual_median': float(np.nanmedian(w['residual']))},
+           'dp_warm_vs_cold_rel': {'median': float(np.median(np.abs(w['dp'][ok] / b['dp'][ok] - 1))),
+                                   'max': float(np.max(np.abs(w['dp'][ok] / b['dp'][ok] - 1)))}}
+    rows = r['plain']
+    if rows:
+        wdp = np.mean([(p['wall_dp_s'] if p['wall_dp_s'] is not None else p['wall_s']) for p in rows])
+        n_ok = int((b['status'] == 'converged').sum())
+        out['plain_fp64'] = {'sample': len(rows), 'wall_per_droplet_s': round(float(wdp), 3),
+                             'wall_extrapolated_s': round(float(wdp * n_ok), 1),
+                             'dp_rel_err_cold': [float(abs(b['dp'][p['index']] / p['dp'] - 1)) for p in rows],
+                             'dp_rel_err_warm': [float(abs(w['dp'][p['index']] / p['dp'] - 1)) for p in rows]}
+        out['speedup_cold'] = round(float(wdp * n_ok / b['wall_s']), 2)
+        out['speedup_warm'] = round(float(wdp * n_ok / w['wall_s']), 2)
     out['total_wall_s'] = round(time.perf_counter() - t0, 1)
     m.close()
     return out
@@ -748,6 +796,8 @@ def main():
     ap.add_argument('--sweep3d-n', type=int, default=256)
     ap.add_argument('--sweep3d-max-steps', type=int, default=20000)
     ap.add_argument('--sweep3d-plain', type=int, default=8)
+    ap.add_argument('--warmstart3d', action='store_true', help='learned warm start of the 3D batched droplets')
+    ap.add_argument('--ws3d-profiles', type=int, default=128)
     ap.add_argument('--ws-profiles', type=int, default=4096)
     ap.add_argument('--ws-max-steps', type=int, default=60000)
     ap.add_argument('--ws-train-steps', type=int, default=20000)
@@ -777,6 +827,9 @@ def main():
         return 0
     if a.sweep3d:
         print(json.dumps(run_sweep3d_mode(a)))
+        return 0
+    if a.warmstart3d:
+        print(json.dumps(run_warmstart3d_mode(a)))
         return 0
     if a.impl == 'reference':
         ws, rank, _ = dist_env()

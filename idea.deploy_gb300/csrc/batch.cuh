@@ -134,25 +134,36 @@ __global__ void __launch_bounds__(BATCH_THREADS) k_batch_mass(const float *__res
     if (I.active) {
         const int V = I.Lx * I.Ly * I.Lz;
         for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < V; g += gridDim.x * blockDim.x) {
-            double s = (double)I.rho0;
+            double s = 0.0;
 #pragma unroll
             for (int q = 0; q < L::Q; q++) s += (double)pop[q * Vtot + I.base + g];
-            v[2] += s;
+            v[1] += fabs(s);  // sum of |n - rho0|: the weights of the mass correction
+            v[2] += s + (double)I.rho0;
         }
     }
     batch_block_reduce(v, partials + ((size_t)blockIdx.y * gridDim.x + blockIdx.x) * BATCH_NV);
 }
 
-// add delta[i] to the rest population (q = 0) of every cell of active lattice i
+// Mass correction of active lattice i: the rest population (q = 0) of every
+// cell gets delta[i] * |n - rho0| of the cell.  FP32 rounding loses mass in
+// proportion to the magnitude of the stored deviations (in the liquid, with
+// the shift at the gas density), so the mass is put back where it was lost;
+// a uniform correction would move mass from the liquid into the gas at every
+// check and disturb the droplet's Laplace pressure.
 template <class L>
 __global__ void __launch_bounds__(BATCH_THREADS) k_batch_add_rest(float *__restrict__ pop,
-                                                                 const BatchInst *__restrict__ inst,
+                                                                 const BatchInst *__restrict__ inst, const int Vtot,
                                                                  const float *__restrict__ delta) {
     const BatchInst I = inst[blockIdx.y];
     const float dl = delta[blockIdx.y];
     if (!I.active || dl == 0.f) return;
     const int V = I.Lx * I.Ly * I.Lz;
-    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < V; g += gridDim.x * blockDim.x) pop[I.base + g] += dl;
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g < V; g += gridDim.x * blockDim.x) {
+        float d = 0.f;
+#pragma unroll
+        for (int q = 0; q < L::Q; q++) d += pop[q * Vtot + I.base + g];
+        pop[I.base + g] += dl * fabsf(d);
+    }
 }
 
 // density (FP64 sum) at the centre cell (L_d / 2 in every dimension) and at

@@ -71,7 +71,7 @@ struct KernelOps {
     // exact per-lattice mass, rest-population correction, centre/last-cell density
     cudaError_t (*batch_mass)(const void *pop, const BatchInst *inst, int n_inst, int Vtot, double *partials, int gx,
                               cudaStream_t st);
-    cudaError_t (*batch_add_rest)(void *pop, const BatchInst *inst, int n_inst, const float *delta, int gx,
+    cudaError_t (*batch_add_rest)(void *pop, const BatchInst *inst, int n_inst, int Vtot, const float *delta, int gx,
                                   cudaStream_t st);
     cudaError_t (*batch_probe)(const void *pop, const BatchInst *inst, int n_inst, int Vtot, double *out, int rad,
                                cudaStream_t st);
@@ -379,10 +379,10 @@ struct Ops {
         }
         return cudaErrorNotSupported;
     }
-    static cudaError_t batch_add_rest(void *pop, const BatchInst *inst, int n_inst, const float *delta, int gx,
-                                      cudaStream_t st) {
+    static cudaError_t batch_add_rest(void *pop, const BatchInst *inst, int n_inst, int Vtot, const float *delta,
+                                      int gx, cudaStream_t st) {
         if constexpr (std::is_same<Real, float>::value) {
-            k_batch_add_rest<L><<<dim3(gx, n_inst), BATCH_THREADS, 0, st>>>((float *)pop, inst, delta);
+            k_batch_add_rest<L><<<dim3(gx, n_inst), BATCH_THREADS, 0, st>>>((float *)pop, inst, Vtot, delta);
             return cudaGetLastError();
         }
         return cudaErrorNotSupported;

@@ -2268,17 +2268,21 @@ int sclbm_batch_restore_mass(sclbm_batch *b, const double *target, double *befor
     bool any = false;
     for (int i = 0; i < b->n; i++) {
         if (b->home[i] >= 0) continue;  // retired
-        double m = 0;
-        for (int k = 0; k < b->gx; k++) m += part[((size_t)i * b->gx + k) * BATCH_NV + 2];
+        double m = 0, w = 0;
+        for (int k = 0; k < b->gx; k++) {
+            m += part[((size_t)i * b->gx + k) * BATCH_NV + 2];
+            w += part[((size_t)i * b->gx + k) * BATCH_NV + 1];
+        }
         if (before) before[i] = m;
-        if (std::isfinite(target[i]) && std::isfinite(m)) {
-            delta[i] = (float)((target[i] - m) / (double)lattice_cells(b, i));
+        // the correction goes to each cell in proportion to |n - rho0|
+        if (std::isfinite(target[i]) && std::isfinite(m) && w > 0) {
+            delta[i] = (float)((target[i] - m) / w);
             any = any || delta[i] != 0.f;
         }
     }
     if (!any) return SCLBM_OK;
     CUDA_TRY(cudaMemcpyAsync(b->delta_d, delta.data(), sizeof(float) * b->n, cudaMemcpyHostToDevice, b->st));
-    e = b->ops->batch_add_rest(b->pop[b->cur], b->inst_d, b->n, b->delta_d, b->gx, b->st);
+    e = b->ops->batch_add_rest(b->pop[b->cur], b->inst_d, b->n, (int)b->Vtot, b->delta_d, b->gx, b->st);
     if (e != cudaSuccess) return fail(SCLBM_ERR_CUDA, "batch mass correction: %s", cudaGetErrorString(e));
     CUDA_TRY(cudaStreamSynchronize(b->st));
     return SCLBM_OK;

@@ -143,10 +143,9 @@ def ragged_sweep(radii, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, che
     for i in range(n):
         b.set_density(i, init[i] if init is not None else cold(i))
     b.init_populations()
-    # the Laplace-pressure probes average a small bulk block (5x5 in 2D, 3x3x3
-    # in 3D): a single FP32 cell's rounding noise is a few 1e-5 of a large
-    # droplet's Laplace pressure, above the criterion's 2e-5
-    b.set_probe_radius((2 if dim == 2 else 1) if probe_rad is None else probe_rad)
+    # the Laplace-pressure probes: single cells, as DeltaPLaplace reads them
+    # (probe_rad > 0 averages a bulk block about each)
+    b.set_probe_radius(0 if probe_rad is None else probe_rad)
     residual = np.full(n, np.nan)
     fallback = np.zeros(n, bool)
     if init is not None and residual_max is not None:
@@ -361,14 +360,18 @@ def run_sweep(n=64, r_min=8, seed=2024, G_range=(-6.0, -4.5), stencil='D2E8', ch
 
 
 def run_sweep3d(n=256, seed=2025, R_range=(10.0, 30.0), G_range=(-6.0, -4.5), L=96, stencil='D3E6', check_every=500,
-                tol_dp=2e-5, tol64=1e-12, max_steps=20000, plain_sample=8, device=0):
+                tol_dp=2e-5, tol64=1e-12, max_steps=20000, plain_sample=8, device=0, mlp=None, residual_max=None,
+                plain_stop_at_dp=False):
     """Batched 3D droplets: n D3Q19 droplets, radius and G uniform in their
     ranges (seeded), each in an L^3 periodic box, FP32-shifted batches (split
     so that Q * cells < 2^31 per batch); then the plain FP64 path, cold
     started, on `plain_sample` of the droplets the batch converged, timed one
     after another.  Start densities: the flat-interface thermodynamic
     construction of the 2D stencil of the same order (sclbm.thermo has the 2D
-    pressure-tensor constants)."""
+    pressure-tensor constants).  With ``mlp`` (a network trained on 3D
+    profiles, warmstart.equilibrium_profiles_3d) the same droplets are run
+    again from its predicted radial profiles (mass-matched to the tanh starts)
+    with the cold-start fallback above ``residual_max``."""
     rng = np.random.default_rng(seed)
     radii = rng.uniform(*R_range, n)
     Gs = rng.uniform(*G_range, n)
@@ -387,18 +390,38 @@ def run_sweep3d(n=256, seed=2025, R_range=(10.0, 30.0), G_range=(-6.0, -4.5), L=
     cat = lambda k: np.concatenate([p[k] for p in parts])
     batch = dict(radii=radii, G=Gs, steps=cat('steps'), status=cat('status'), dp=cat('dp'), max_u=cat('max_u'),
                  wall_s=wall, batches=[len(g) for g in groups])
+    warm = None
+    if mlp is not None:
+        from .warmstart import warm_fields
+        t1 = time.perf_counter()
+        wparts = []
+        for gi in groups:
+            masses = [droplet((L,) * 3, float(radii[i]), rl[i], rg[i], 2.0, seed + k, 0.0).sum()
+                      for k, i in enumerate(gi)]
+            fields = warm_fields(mlp, [float(radii[i]) for i in gi], [float(Gs[i]) for i in gi], tau=1.0,
+                                 order=int(stencil[-1]), masses=masses, dim=3, box=L)
+            wparts.append(ragged_sweep([float(radii[i]) for i in gi], [float(Gs[i]) for i in gi],
+                                       [rl[i] for i in gi], [rg[i] for i in gi], stencil=stencil,
+                                       check_every=check_every, tol_dp=tol_dp, max_steps=max_steps, device=device,
+                                       dim=3, boxes=[L] * len(gi), seed=seed, init=fields,
+                                       residual_max=residual_max))
+            del fields
+        wcat = lambda k: np.concatenate([p[k] for p in wparts])
+        warm = dict(steps=wcat('steps'), status=wcat('status'), dp=wcat('dp'), residual=wcat('residual'),
+                    fallback=wcat('fallback'), wall_s=time.perf_counter() - t1)
     ok = np.nonzero(batch['status'] == 'converged')[0]
     pick = rng.choice(ok, size=min(plain_sample, len(ok)), replace=False) if len(ok) else []
     plain = []
     for i in pick:
         r = plain_run(float(radii[i]), float(Gs[i]), rl[i], rg[i], stencil=stencil, check_every=check_every,
-                      tol=tol64, max_steps=max_steps, device=device, dim=3, L=L, seed=seed + int(i))
+                      tol=tol64, max_steps=max_steps, device=device, dim=3, L=L, seed=seed + int(i),
+                      tol_dp=tol_dp, stop_at_dp=plain_stop_at_dp)
         r['index'] = int(i)
         plain.append(r)
     return dict(config=dict(n=n, seed=seed, R_range=list(R_range), G_range=list(G_range), box=L, stencil=stencil,
                             tau=1.0, check_every=check_every, tol_dp_fp32=tol_dp, tol_u_fp64=tol64,
                             max_steps=max_steps, plain_sample=len(plain)),
-                batch=batch, plain=plain, rho_l=rl, rho_g=rg)
+                batch=batch, plain=plain, rho_l=rl, rho_g=rg, warm=warm)
 
 
 # late import (batch imports MultiPhase, which imports this package's _lib)

@@ -125,11 +125,44 @@ def equilibrium_profiles(n=4096, seed=7, max_steps=60000, check_every=500, tol_d
     return prof, dict(wall_s=wall, status=st)
 
 
-def split(profiles, holdout=512, seed=0):
+def equilibrium_profiles_3d(n=128, seed=11, R_range=(10.0, 30.0), G_range=(-6.0, -4.5), L=96, stencil='D3E6',
+                            max_steps=20000, check_every=500, tol_dp=2e-5, device=0):
+    """Plain-method equilibrium profiles of n seeded 3D droplets (D3Q19, tau 1,
+    cubic boxes of side L), in FP32 batches of at most 2^31 population values;
+    start densities from the thermodynamic construction of the 2D stencil of
+    the same order, as sweep.run_sweep3d starts them."""
+    rng = np.random.default_rng(seed)
+    R = rng.uniform(*R_range, n)
+    G = rng.uniform(*G_range, n)
+    guess = [sweep.thermo_guess(g, 'D2E' + stencil[-1]) or (4.6, 0.2) for g in G]
+    per = max(1, ((1 << 31) - 1) // (19 * L ** 3) - 1)
+    prof = []
+    t0 = time.perf_counter()
+    for gi in np.array_split(np.arange(n), int(math.ceil(n / per))):
+        r = sweep.ragged_sweep([float(R[i]) for i in gi], [float(G[i]) for i in gi], [guess[i][0] for i in gi],
+                               [guess[i][1] for i in gi], stencil=stencil, check_every=check_every, tol_dp=tol_dp,
+                               max_steps=max_steps, device=device, dim=3, boxes=[L] * len(gi), seed=seed,
+                               return_fields=True)
+        for j, i in enumerate(gi):
+            p = dict(G=float(G[i]), tau=1.0, R=float(R[i]), order=int(stencil[-1]), status=str(r['status'][j]),
+                     steps=int(r['steps'][j]), dp=float(r['dp'][j]))
+            if p['status'] == 'converged':
+                p['r'], p['rho'] = radial_profile(r['fields'][j])
+            prof.append(p)
+        del r
+    st = {}
+    for p in prof:
+        st[p['status']] = st.get(p['status'], 0) + 1
+    return prof, dict(wall_s=time.perf_counter() - t0, status=st)
+
+
+def split(profiles, holdout=512, seed=0, min_train_share=0.5):
+    """(train, held out): `holdout` converged profiles held out, or fewer when
+    that would leave less than min_train_share of them for training."""
     ok = [p for p in profiles if p['status'] == 'converged']
     rng = np.random.default_rng(seed)
     perm = rng.permutation(len(ok))
-    k = min(holdout, len(ok) // 4)
+    k = min(holdout, int(len(ok) * (1 - min_train_share)))
     return [ok[i] for i in perm[k:]], [ok[i] for i in perm[:k]]
 
 
@@ -174,20 +207,22 @@ def evaluate(m, profiles):
                 coexistence_rel_err_gas={'median': float(np.median(cout)), 'max': float(np.max(cout))})
 
 
-def warm_fields(m, radii, G, tau=1.0, order=8, dr=0.02, masses=None, iterations=4):
-    """Initial density fields (box 4R rounded up to 32) from the predicted
-    radial profiles, linearly interpolated in r.  The profiles are learned for
-    r <= L/2; the corners beyond take the value at L/2.  With ``masses`` the
-    radius fed to the network is adjusted (Newton steps on M(R)) until each
-    field carries that mass, so the extra or missing mass goes into the size of
-    the droplet, not into its bulk densities."""
-    boxes = [box_of(R) for R in radii]
-    grids = [np.arange(0.0, L / 2 + 2 * dr, dr) for L in boxes]
-    rfield = [radius_field((L, L)) for L in boxes]
+def warm_fields(m, radii, G, tau=1.0, order=8, dr=0.02, masses=None, iterations=4, dim=2, box=None):
+    """Initial density fields (box 4R rounded up to 32, or ``box``) from the
+    predicted radial profiles, linearly interpolated in r.  The profiles are
+    learned for r <= L/2; the corners beyond take the value at L/2.  With
+    ``masses`` the radius fed to the network is adjusted (Newton steps on M(R))
+    until each field carries that mass, so the extra or missing mass goes into
+    the size of the droplet, not into its bulk densities.  dim = 3: spherical
+    droplets in cubic boxes (a network trained on 3D profiles)."""
+    boxes = [box or box_of(R) for R in radii]
+    grids = [np.arange(0.0, L * (math.sqrt(dim) / 2) + 2 * dr, dr) for L in boxes]
+    rfield = [radius_field((L,) * dim) for L in boxes]
 
     def fields_for(Rs):
-        y = from_target(m.predict(np.concatenate([features(g, tau, R, order, rg)
-                                                  for R, g, rg in zip(Rs, G, grids)])))
+        # the network saw r <= L/2 only: beyond, the value at L/2
+        y = from_target(m.predict(np.concatenate([features(g, tau, R, order, np.minimum(rg, L / 2))
+                                                  for R, g, rg, L in zip(Rs, G, grids, boxes)])))
         out, k = [], 0
         for rg, rf in zip(grids, rfield):
             out.append(np.interp(rf, rg, y[k:k + len(rg)]))
@@ -200,9 +235,10 @@ def warm_fields(m, radii, G, tau=1.0, order=8, dr=0.02, masses=None, iterations=
         return out
     for _ in range(iterations):
         mass = np.array([f.sum() for f in out])
-        # dM/dR of a disc of liquid in gas: 2 pi R (rho_in - rho_out)
-        drho = np.array([f[f.shape[0] // 2, f.shape[1] // 2] - f[-1, -1] for f in out])
-        step = (np.asarray(masses) - mass) / np.maximum(2 * np.pi * Rs * drho, 1e-6)
+        # dM/dR of a disc (sphere) of liquid in gas: 2 pi R (4 pi R^2) times (rho_in - rho_out)
+        drho = np.array([f[tuple(n // 2 for n in f.shape)] - f[(-1,) * dim] for f in out])
+        area = 2 * np.pi * Rs if dim == 2 else 4 * np.pi * Rs ** 2
+        step = (np.asarray(masses) - mass) / np.maximum(area * drho, 1e-6)
         Rs = np.clip(Rs + step, 0.5 * np.asarray(radii), 1.5 * np.asarray(radii))
         out = fields_for(Rs)
     return out

@@ -366,9 +366,12 @@ SCLBM_API int sclbm_batch_check(sclbm_batch *b, double *u_conv, double *max_u, d
 SCLBM_API int sclbm_batch_set_active(sclbm_batch *b, const int *active);
 /* steps each lattice has taken */
 SCLBM_API int sclbm_batch_steps(const sclbm_batch *b, int64_t *steps);
-/* sclbm_restore_mass per active lattice: before[i] = its FP64 mass; where
- * target[i] is finite, (target[i] - mass) / V_i is added to its rest
- * populations. */
+/* mass restoration per active lattice: before[i] = its FP64 mass; where
+ * target[i] is finite, target[i] - mass is added to its rest populations,
+ * to each cell in proportion to |n - rho0| of the cell (FP32 rounding loses
+ * mass where the stored deviations are large, i.e. in the liquid when rho0 is
+ * the gas density; a uniform correction would move mass from the droplet into
+ * the gas at every check). */
 SCLBM_API int sclbm_batch_restore_mass(sclbm_batch *b, const double *target, double *before);
 /* density (FP64 sum of the populations) at the centre cell (L_d / 2 in every
  * dimension) and at the last cell of every active lattice: the two densities
@@ -377,10 +380,11 @@ SCLBM_API int sclbm_batch_restore_mass(sclbm_batch *b, const double *target, dou
 SCLBM_API int sclbm_batch_probe(sclbm_batch *b, double *n_in, double *n_out);
 /* make sclbm_batch_probe return the mean density over the cube (square in 2D)
  * of side 2 rad + 1 about each probe cell, rad in [0, 4] (0, the default: the
- * single cell).  For FP32-shifted storage: the rounding noise of one cell's
- * stored populations (~1e-7 of the liquid density) is a few 1e-5 of the Laplace
- * pressure of a large droplet; the mean over 25 or 27 bulk cells, which agree
- * in equilibrium, lowers it about five-fold.  No counterpart in the reference. */
+ * single cell, as the reference's DeltaPLaplace reads them).  A block mean
+ * lowers the FP32 rounding noise of a single probe cell; in equilibrium the
+ * bulk cells agree, but spurious-current structure near the droplet centre
+ * biases the mean by ~1e-5 of the Laplace pressure, so the sweeps keep single
+ * cells.  No counterpart in the reference. */
 SCLBM_API int sclbm_batch_set_probe_radius(sclbm_batch *b, int rad);
 
 /* ---------------------------------------------------------------------------

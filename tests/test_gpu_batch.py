@@ -132,7 +132,7 @@ def test_batch_probe_block_means():
         nf = b.get_density(i)
         cy, cx = d[1] // 2, d[0] // 2
         blk = nf[cy - 2:cy + 3, cx - 2:cx + 3]
-        corner = np.roll(np.roll(nf, 2, axis=0), 2, axis=1)[-5:, -5:]   # rows/cols L-3 .. L+1 (periodic)
+        corner = np.roll(np.roll(nf, -2, axis=0), -2, axis=1)[-5:, -5:]   # rows/cols L-3 .. L+1 (periodic)
         assert abs(ni[i] - blk.mean()) < 1e-12 * abs(ni[i])
         assert abs(no[i] - corner.mean()) < 1e-12 * abs(no[i])
     b.close()
