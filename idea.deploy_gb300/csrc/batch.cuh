@@ -137,7 +137,7 @@ __global__ void __launch_bounds__(BATCH_THREADS) k_batch_mass(const float *__res
             double s = 0.0;
 #pragma unroll
             for (int q = 0; q < L::Q; q++) s += (double)pop[q * Vtot + I.base + g];
-            v[1] += fabs(s);  // sum of |n - rho0|: the weights of the mass correction
+            v[0] += fabs(s);  // sum of |n - rho0|: the weights of the mass correction (slot 0 sums)
             v[2] += s + (double)I.rho0;
         }
     }

@@ -2271,7 +2271,7 @@ int sclbm_batch_restore_mass(sclbm_batch *b, const double *target, double *befor
         double m = 0, w = 0;
         for (int k = 0; k < b->gx; k++) {
             m += part[((size_t)i * b->gx + k) * BATCH_NV + 2];
-            w += part[((size_t)i * b->gx + k) * BATCH_NV + 1];
+            w += part[((size_t)i * b->gx + k) * BATCH_NV + 0];
         }
         if (before) before[i] = m;
         // the correction goes to each cell in proportion to |n - rho0|
