@@ -709,9 +709,12 @@ struct BatchInst {
 };
 
 // PAIRS: every lattice has an even Lx and an even first cell (base) and the
-// total volume is even, so the paired halo loads of fused_tile stay aligned
+// total volume is even, so the paired halo loads of fused_tile stay aligned.
+// Resident CTAs per SM as the single-lattice kernel's: four (BGK, paired
+// loads, 64 registers) or three (BGK, one halo cell per load, 80 registers),
+// no spills; two for the dense MRT operator.
 template <class L, class S, bool MRT, bool PAIRS = false>
-__global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
+__global__ void __launch_bounds__(FusedShape<L, S>::NT, MRT ? 2 : (PAIRS ? 4 : 3))
     k_fused_batch(const float *__restrict__ pop, float *__restrict__ pop_out,
                   const __grid_constant__ StepParams<L, S, float> p, const BatchInst *__restrict__ inst,
                   const int4 *__restrict__ items, const int n_items, const int Vtot, int *counter, const int parity) {

@@ -2268,15 +2268,11 @@ int sclbm_batch_restore_mass(sclbm_batch *b, const double *target, double *befor
     bool any = false;
     for (int i = 0; i < b->n; i++) {
         if (b->home[i] >= 0) continue;  // retired
-        double m = 0, w = 0;
-        for (int k = 0; k < b->gx; k++) {
-            m += part[((size_t)i * b->gx + k) * BATCH_NV + 2];
-            w += part[((size_t)i * b->gx + k) * BATCH_NV + 0];
-        }
+        double m = 0;
+        for (int k = 0; k < b->gx; k++) m += part[((size_t)i * b->gx + k) * BATCH_NV + 2];
         if (before) before[i] = m;
-        // the correction goes to each cell in proportion to |n - rho0|
-        if (std::isfinite(target[i]) && std::isfinite(m) && w > 0) {
-            delta[i] = (float)((target[i] - m) / w);
+        if (std::isfinite(target[i]) && std::isfinite(m)) {
+            delta[i] = (float)((target[i] - m) / (double)lattice_cells(b, i));
             any = any || delta[i] != 0.f;
         }
     }

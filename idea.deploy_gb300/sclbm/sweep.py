@@ -282,7 +282,13 @@ def laplace_fit(G=-4.5, radii=(12, 16, 20, 24, 32, 40, 48), stencil='D2E8', devi
 
     sigma, c = fit(r['radii'].astype(float))
     sigma_eq, c_eq = fit(req)
+    # the curvature (Tolman) correction of the 2D Laplace law instead of a
+    # constant offset: dP R = sigma + b / R, fitted on the equimolar radii; a
+    # free intercept in dP = sigma / R + c absorbs the 1/R^2 term and lowers sigma
+    M = np.stack([np.ones(ok.sum()), 1.0 / req[ok]], 1)
+    (sigma_t, b_t), *_ = np.linalg.lstsq(M, r['dp'][ok] * req[ok], rcond=None)
     return dict(G=G, sigma=sigma, intercept=c, sigma_equimolar=sigma_eq, intercept_equimolar=c_eq,
+                sigma_tolman=float(sigma_t), tolman_b=float(b_t),
                 sigma_thermo=th['sigma_f'], radii=[int(v) for v in r['radii']],
                 radii_equimolar=[float(v) for v in req], dp=[float(v) for v in r['dp']],
                 n_in=[float(v) for v in r['n_in']], n_out=[float(v) for v in r['n_out']],

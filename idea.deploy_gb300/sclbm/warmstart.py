@@ -156,7 +156,7 @@ def equilibrium_profiles_3d(n=128, seed=11, R_range=(10.0, 30.0), G_range=(-6.0,
     return prof, dict(wall_s=time.perf_counter() - t0, status=st)
 
 
-def split(profiles, holdout=512, seed=0, min_train_share=0.5):
+def split(profiles, holdout=512, seed=0, min_train_share=0.4):
     """(train, held out): `holdout` converged profiles held out, or fewer when
     that would leave less than min_train_share of them for training."""
     ok = [p for p in profiles if p['status'] == 'converged']

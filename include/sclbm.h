@@ -366,12 +366,9 @@ SCLBM_API int sclbm_batch_check(sclbm_batch *b, double *u_conv, double *max_u, d
 SCLBM_API int sclbm_batch_set_active(sclbm_batch *b, const int *active);
 /* steps each lattice has taken */
 SCLBM_API int sclbm_batch_steps(const sclbm_batch *b, int64_t *steps);
-/* mass restoration per active lattice: before[i] = its FP64 mass; where
- * target[i] is finite, target[i] - mass is added to its rest populations,
- * to each cell in proportion to |n - rho0| of the cell (FP32 rounding loses
- * mass where the stored deviations are large, i.e. in the liquid when rho0 is
- * the gas density; a uniform correction would move mass from the droplet into
- * the gas at every check). */
+/* sclbm_restore_mass per active lattice: before[i] = its FP64 mass; where
+ * target[i] is finite, (target[i] - mass) / V_i is added to its rest
+ * populations. */
 SCLBM_API int sclbm_batch_restore_mass(sclbm_batch *b, const double *target, double *before);
 /* density (FP64 sum of the populations) at the centre cell (L_d / 2 in every
  * dimension) and at the last cell of every active lattice: the two densities
