@@ -239,8 +239,22 @@ SCLBM_HD constexpr int opposite_e(int a) {
 // the caller passes the input's tensor map, the two mbarriers, the running
 // issue / wait counts of own-population boxes (k_issue-th box: buffer k & 1,
 // phase (k >> 1) & 1, the same on every thread) and the error flag.
+// error-free sum (Knuth's TwoSum): a + b = s + e exactly, s the rounded sum
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
+    s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+}
+
+// EXACT_REST: the rest population balances the cell's mass with the rounding
+// errors of the density sum and of the subtraction chain carried along
+// (TwoSum), so that a cell's stored FP32 populations sum to its incoming ones
+// up to one rounding of the rest population.  Without it the ~36 roundings
+// per cell repeat in a near-steady state and drift the mass by ~1e-9 per
+// step; the batched sweeps use it (their Laplace-pressure criterion sees that
+// drift on large droplets).  The density used by the physics is unchanged.
 template <class L, class S, bool MRT, class ST = void, bool WALLS = false, bool PAIRS = false, int STG = 0,
-          int TXT = 0, int TYT = 0>
+          int TXT = 0, int TYT = 0, bool EXACT_REST = false>
 __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float *__restrict__ pop_out, const int V,
                                            const int Lx, const int Ly, const int Lz, const int x0, const int y0,
                                            const int m0, const int m1, const float neg_g, const float rho0,
@@ -511,9 +525,17 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
 #pragma unroll
                 for (int q = 0; q < Q; q++) pop_out[g + q * V] = f[q];
             } else {
-            float d = f[lex_q<Q>(0)];
+            float d = f[lex_q<Q>(0)], d_lo = 0.f;
 #pragma unroll
-            for (int i = 1; i < Q; i++) d += f[lex_q<Q>(i)];
+            for (int i = 1; i < Q; i++) {
+                if constexpr (EXACT_REST) {
+                    float e;
+                    two_sum(d, f[lex_q<Q>(i)], d, e);
+                    d_lo += e;
+                } else {
+                    d += f[lex_q<Q>(i)];
+                }
+            }
             // Shan-Chen force from the psi ring (compile-time offsets); the
             // stencil is symmetric (w_a = w_-a, checked on the host), so each
             // pair +-e_a contributes w_a e_a (psi(x+e_a) - psi(x-e_a))
@@ -548,7 +570,7 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
             }
             const float C0 = p.omega * d - p.om15 * n * u2 - p.fd * uF;
             const float a = p.om45 * n, b = p.om3 * n;
-            float rest_pop = d;
+            float rest_pop = d, rest_lo = d_lo;
             float pend[Q];  // BGK: a direction's result computed with its opposite's
 #pragma unroll
             for (int q = 1; q < Q; q++) {
@@ -566,7 +588,13 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
                 // __fsub_rn: no contraction with the product that made `out`
                 // (at omega = 1 it is a plain multiply), so the rest population
                 // balances exactly the rounded values that are stored
-                rest_pop = __fsub_rn(rest_pop, out);
+                if constexpr (EXACT_REST) {
+                    float e;
+                    two_sum(rest_pop, -out, rest_pop, e);
+                    rest_lo += e;
+                } else {
+                    rest_pop = __fsub_rn(rest_pop, out);
+                }
                 int dst = X3[L::xi(q, 0) + 1] + Y3[L::xi(q, 1) + 1] + Z3[L::xi(q, D - 1) + 1];
                 int qd = q;
                 if constexpr (WALLS) {
@@ -577,7 +605,7 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
                 }
                 pop_out[dst + qd * V] = out;
             }
-            pop_out[g] = rest_pop;
+            pop_out[g] = EXACT_REST ? __fadd_rn(rest_pop, rest_lo) : rest_pop;
             }
         }
     }
@@ -731,7 +759,8 @@ __global__ void __launch_bounds__(FusedShape<L, S>::NT, MRT ? 2 : (PAIRS ? 4 : 3
         const int4 w = items[it];  // lattice, x0, y0, m0 | m1 << 16
         const BatchInst I = inst[w.x];
         if (!I.active) continue;
-        fused_tile<L, S, MRT, void, false, PAIRS>(pop + I.base, pop_out + I.base, Vtot, I.Lx, I.Ly, I.Lz, w.y, w.z,
+        fused_tile<L, S, MRT, void, false, PAIRS, 0, 0, 0, true>(pop + I.base, pop_out + I.base, Vtot, I.Lx, I.Ly,
+                                                                 I.Lz, w.y, w.z,
                                                   w.w & 0xffff, w.w >> 16, I.neg_g, I.rho0, p, smem);
     }
 }
