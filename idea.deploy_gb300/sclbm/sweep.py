@@ -199,7 +199,7 @@ def ragged_sweep(radii, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, che
                    for h, st in zip(hist, status)])
     return dict(radii=np.array(radii), boxes=np.array(boxes), G=np.array(G), steps=steps, u_conv=u_conv,
                 max_u=max_u, status=status, dp=dp, n_in=n_in, n_out=n_out, wall_s=wall, residual=residual,
-                fallback=fallback, fields=fields)
+                fallback=fallback, fields=fields, dp_history=hist)
 
 
 def plain_run(R, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, check_every=500, tol=1e-12,
