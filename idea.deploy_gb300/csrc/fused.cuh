@@ -42,11 +42,14 @@ enum : int { STG_HALO_ASYNC = 1, STG_OWN_TMA = 2 };
 // 64 x 8 and 32 x 16 (512 threads, two CTAs per SM), 128 x 8 (1024 threads,
 // one).  Every shape computes the same cells with the same arithmetic, so the
 // results are bit-identical; the autotuner picks among them.
+// Shape 4 is the default shape with streaming stores (st.global.cs: the
+// pushed populations are not read again within the step, so they are marked
+// evict-first and leave L2 to the halo lines that neighbouring tiles re-read).
 struct TileShape {
-    int tx, ty, minb;
+    int tx, ty, minb, cs;
 };
-constexpr TileShape kTiles[] = {{32, 8, 4}, {64, 8, 2}, {32, 16, 2}, {128, 8, 1}};
-constexpr int N_TILES = 4;
+constexpr TileShape kTiles[] = {{32, 8, 4, 0}, {64, 8, 2, 0}, {32, 16, 2, 0}, {128, 8, 1, 0}, {32, 8, 4, 1}};
+constexpr int N_TILES = 5;
 
 template <class L, class S, int TXp = 0, int TYp = 0>
 struct FusedShape {
@@ -150,6 +153,7 @@ struct FusedGeom {
     int pairs;  // 3D, even Lx and even halo radius: halo populations loaded two cells per load
     int stg;    // STG_* flags of the staged 3D variants (0: none)
     int tile;   // index into kTiles (3D paired BGK; 0: the default shape)
+    int order;  // order of the work items over the grid (k_fused; 0 x, 1 chunk, 2 y fastest)
     int *err;   // device flag set by a staged variant whose bounded wait gave up
 };
 
@@ -254,7 +258,7 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
 // step; the batched sweeps use it (their Laplace-pressure criterion sees that
 // drift on large droplets).  The density used by the physics is unchanged.
 template <class L, class S, bool MRT, class ST = void, bool WALLS = false, bool PAIRS = false, int STG = 0,
-          int TXT = 0, int TYT = 0, bool EXACT_REST = false>
+          int TXT = 0, int TYT = 0, bool EXACT_REST = false, bool CS = false>
 __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float *__restrict__ pop_out, const int V,
                                            const int Lx, const int Ly, const int Lz, const int x0, const int y0,
                                            const int m0, const int m1, const float neg_g, const float rho0,
@@ -603,9 +607,12 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
                         qd = opposite_q<L>(q);
                     }
                 }
-                pop_out[dst + qd * V] = out;
+                if constexpr (CS) __stcs(pop_out + (dst + qd * V), out);
+                else pop_out[dst + qd * V] = out;
             }
-            pop_out[g] = EXACT_REST ? __fadd_rn(rest_pop, rest_lo) : rest_pop;
+            const float rest_out = EXACT_REST ? __fadd_rn(rest_pop, rest_lo) : rest_pop;
+            if constexpr (CS) __stcs(pop_out + g, rest_out);
+            else pop_out[g] = rest_out;
             }
         }
     }
@@ -627,14 +634,30 @@ __global__ void __launch_bounds__(TILE ? kTiles[TILE].tx * kTiles[TILE].ty : Fus
     extern __shared__ float smem[];
     const int Lm = D == 3 ? fg.L[2] : fg.L[1];
     for (int item = blockIdx.x; item < fg.items; item += gridDim.x) {
-        const int ix = item % fg.tiles_x;
-        const int rest = item / fg.tiles_x;
-        const int iy = D == 3 ? rest % fg.tiles_y : 0;
-        const int ic = D == 3 ? rest / fg.tiles_y : rest;
+        // order of the work items over the grid: 0 x fastest, then y, then
+        // the chunk; 1 the chunk fastest (a tile column's chunks together);
+        // 2 y fastest
+        int ix, iy, ic;
+        if (fg.order == 1) {
+            ic = item % fg.chunks;
+            const int r = item / fg.chunks;
+            ix = r % fg.tiles_x;
+            iy = D == 3 ? r / fg.tiles_x : 0;
+        } else if (fg.order == 2 && D == 3) {
+            iy = item % fg.tiles_y;
+            const int r = item / fg.tiles_y;
+            ix = r % fg.tiles_x;
+            ic = r / fg.tiles_x;
+        } else {
+            ix = item % fg.tiles_x;
+            const int rest = item / fg.tiles_x;
+            iy = D == 3 ? rest % fg.tiles_y : 0;
+            ic = D == 3 ? rest / fg.tiles_y : rest;
+        }
         const int m0 = ic * fg.chunk;
-        fused_tile<L, S, MRT, void, false, PAIRS, 0, TXT, TYT>(pop, pop_out, (int)fg.V, fg.L[0], fg.L[1], fg.L[2],
-                                                               ix * SH::TX, iy * SH::TY, m0, min(m0 + fg.chunk, Lm),
-                                                               p.neg_g, p.rho0, p, smem);
+        fused_tile<L, S, MRT, void, false, PAIRS, 0, TXT, TYT, false, kTiles[TILE].cs != 0>(
+            pop, pop_out, (int)fg.V, fg.L[0], fg.L[1], fg.L[2], ix * SH::TX, iy * SH::TY, m0, min(m0 + fg.chunk, Lm),
+            p.neg_g, p.rho0, p, smem);
     }
 }
 

@@ -257,6 +257,7 @@ struct Ops {
                 if (fg.pairs && !fg.stg && fg.tile == 1) return launch_tile<1>(pop, pop_out, sp, fg, grid, st);
                 if (fg.pairs && !fg.stg && fg.tile == 2) return launch_tile<2>(pop, pop_out, sp, fg, grid, st);
                 if (fg.pairs && !fg.stg && fg.tile == 3) return launch_tile<3>(pop, pop_out, sp, fg, grid, st);
+                if (fg.pairs && !fg.stg && fg.tile == 4) return launch_tile<4>(pop, pop_out, sp, fg, grid, st);
             }
             if (fg.stg || fg.tile) return cudaErrorNotSupported;
             if constexpr (L::D == 3 && S::R % 2 == 0) {
@@ -308,6 +309,7 @@ struct Ops {
                 if (pairs && tile == 1) return occupancy_tile<1>();
                 if (pairs && tile == 2) return occupancy_tile<2>();
                 if (pairs && tile == 3) return occupancy_tile<3>();
+                if (pairs && tile == 4) return occupancy_tile<4>();
             }
             int b = 0;
             if constexpr (L::D == 3 && S::R % 2 == 0) {

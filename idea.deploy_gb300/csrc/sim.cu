@@ -256,6 +256,7 @@ struct sclbm_sim {
     int fused_grid = 0, path = SCLBM_PATH_AUTO, chunk_override = 0;
     int staging = -1;  // requested SCLBM_STAGE_* flags of the 3D single pass (-1: automatic)
     int tile = -1;     // requested tile shape (index into kTiles) of the 3D paired single pass (-1: automatic)
+    int item_order = -1;  // requested order of the single pass's work items (-1: automatic, 0)
     // tensor maps of the two population buffers (4D: x, y, plane, q; box of one
     // tile plane), encoded when a staged variant with TMA loads is planned
     CUtensorMap tmap[2];
@@ -552,16 +553,19 @@ void plan_fused(sclbm_sim *s) {
     if (!o->fused) return;
     sclbm_tuning tuned;
     if (s->path == SCLBM_PATH_AUTO && s->chunk_override == 0 && s->staging < 0 && cached_tuning(s, &tuned)) {
-        const int saved_path = s->path, saved_chunk = s->chunk_override, saved_stg = s->staging, saved_tile = s->tile;
+        const int saved_path = s->path, saved_chunk = s->chunk_override, saved_stg = s->staging, saved_tile = s->tile,
+                  saved_order = s->item_order;
         s->path = tuned.path == SCLBM_PATH_FUSED ? SCLBM_PATH_FUSED : SCLBM_PATH_AUTO;
         s->chunk_override = tuned.chunk;
         s->staging = tuned.staging;
         s->tile = tuned.tile;
+        s->item_order = tuned.order;
         plan_fused(s);
         s->path = saved_path;
         s->chunk_override = saved_chunk;
         s->staging = saved_stg;
         s->tile = saved_tile;
+        s->item_order = saved_order;
         return;
     }
     FusedGeom &g = s->fg;
@@ -585,6 +589,7 @@ void plan_fused(sclbm_sim *s) {
         g.tiles_x = (s->L[0] + kTiles[g.tile].tx - 1) / kTiles[g.tile].tx;
         g.tiles_y = (s->L[1] + kTiles[g.tile].ty - 1) / kTiles[g.tile].ty;
     }
+    g.order = (s->item_order > 0 && s->item_order <= 2 && !s->walls && !s->noise_kind && !g.stg) ? s->item_order : 0;
     const int resident = s->sms * (s->noise_kind ? o->fused_noise_occupancy()
                                    : s->walls    ? o->fused_walls_occupancy()
                                                  : o->fused_occupancy(g.pairs, g.stg, g.tile));
@@ -1299,13 +1304,16 @@ int sclbm_set_tuning_ex(sclbm_sim *s, const sclbm_tuning *t) {
     if (t->staging < -1 || t->staging > (SCLBM_STAGE_HALO_ASYNC | SCLBM_STAGE_OWN_TMA))
         return fail(SCLBM_ERR_ARG, "staging %d", t->staging);
     if (t->tile < -1 || t->tile >= N_TILES) return fail(SCLBM_ERR_ARG, "tile %d (0 .. %d)", t->tile, N_TILES - 1);
-    const int saved = s->staging, saved_tile = s->tile;
+    if (t->order < -1 || t->order > 2) return fail(SCLBM_ERR_ARG, "order %d (0 .. 2)", t->order);
+    const int saved = s->staging, saved_tile = s->tile, saved_order = s->item_order;
     s->staging = t->staging;
     s->tile = t->tile;
+    s->item_order = t->order;
     const int rc = sclbm_set_tuning(s, t->path, t->chunk);
     if (rc) {
         s->staging = saved;
         s->tile = saved_tile;
+        s->item_order = saved_order;
     }
     return rc;
 }
@@ -1315,6 +1323,7 @@ int sclbm_get_tuning_ex(const sclbm_sim *s, sclbm_tuning *t) {
     sclbm_get_tuning(s, &t->path, &t->chunk, &t->grid);
     t->staging = fused_path(s) ? s->fg.stg : 0;
     t->tile = fused_path(s) ? s->fg.tile : 0;
+    t->order = fused_path(s) ? s->fg.order : 0;
     return SCLBM_OK;
 }
 
@@ -1339,13 +1348,14 @@ int sclbm_autotune(sclbm_sim *s, int trial_steps, sclbm_tuning *best, double *be
                                            "write the current populations)");
     DevGuard dg(s->device);
     CUDA_TRY(cudaStreamSynchronize(s->st));
-    const int saved_path = s->path, saved_chunk = s->chunk_override, saved_stg = s->staging, saved_tile = s->tile;
+    const int saved_path = s->path, saved_chunk = s->chunk_override, saved_stg = s->staging, saved_tile = s->tile,
+              saved_order = s->item_order;
     struct Cand {
-        int path, chunk, staging, tile;
+        int path, chunk, staging, tile, order;
     };
     std::vector<Cand> cands;
     if (!fused_path(s)) {
-        cands.push_back({s->path, 0, 0, 0});
+        cands.push_back({s->path, 0, 0, 0, 0});
     } else {
         const int Lm = s->D == 3 ? s->L[2] : s->L[1];
         const bool pairs_ok = s->D == 3 && s->L[0] % 2 == 0 && s->ops->fused_r % 2 == 0 && !s->walls;
@@ -1357,12 +1367,12 @@ int sclbm_autotune(sclbm_sim *s, int trial_steps, sclbm_tuning *best, double *be
         for (int path : paths) {
             for (int stg = 0; stg <= 3; stg++) {
                 if (stg && (path != SCLBM_PATH_FUSED_PAIRS || !(s->ops->fused_stg_mask & stg))) continue;
-                for (int c : chunks) cands.push_back({path, c, stg, 0});
+                for (int c : chunks) cands.push_back({path, c, stg, 0, 0});
             }
             if (path == SCLBM_PATH_FUSED_PAIRS)
                 for (int tile = 1; tile < N_TILES; tile++)
                     if (s->ops->fused_tile_mask >> tile & 1)
-                        for (int c : chunks) cands.push_back({path, c, 0, tile});
+                        for (int c : chunks) cands.push_back({path, c, 0, tile, 0});
         }
     }
     cudaEvent_t e0, e1;
@@ -1370,17 +1380,22 @@ int sclbm_autotune(sclbm_sim *s, int trial_steps, sclbm_tuning *best, double *be
     CUDA_TRY(cudaEventCreate(&e1));
     double best_t = 1e300;
     Cand win = cands[0];
-    std::vector<std::array<int, 5>> seen;  // effective (pairs, staging, tile, chunk, grid) already timed
+    std::vector<std::array<int, 6>> seen;  // effective (pairs, staging, tile, chunk, grid, order) already timed
     int rc = SCLBM_OK;
-    for (const Cand &c : cands) {
+    // two stages: every variant in the default item order, then the other
+    // orders of the winner
+    bool orders_added = false;
+    for (size_t ci = 0; ci < cands.size(); ci++) {
+        const Cand c = cands[ci];
         s->path = c.path;
         s->chunk_override = c.chunk;
         s->staging = c.staging;
         s->tile = c.tile;
+        s->item_order = c.order;
         plan_fused(s);
         const bool fp = fused_path(s);
-        const std::array<int, 5> eff = {fp ? s->fg.pairs : -1, fp ? s->fg.stg : -1, fp ? s->fg.tile : -1,
-                                        fp ? s->fg.chunk : 0, fp ? s->fused_grid : 0};
+        const std::array<int, 6> eff = {fp ? s->fg.pairs : -1, fp ? s->fg.stg : -1, fp ? s->fg.tile : -1,
+                                        fp ? s->fg.chunk : 0, fp ? s->fused_grid : 0, fp ? s->fg.order : 0};
         if (std::find(seen.begin(), seen.end(), eff) != seen.end()) continue;
         seen.push_back(eff);
         // one untimed launch, then trial_steps timed ones, all from the current buffer
@@ -1400,6 +1415,10 @@ int sclbm_autotune(sclbm_sim *s, int trial_steps, sclbm_tuning *best, double *be
             best_t = ms;
             win = c;
         }
+        if (ci + 1 == cands.size() && !orders_added && fused_path(s) && cands.size() > 1) {
+            orders_added = true;
+            for (int order = 1; order <= 2; order++) cands.push_back({win.path, win.chunk, win.staging, win.tile, order});
+        }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -1409,6 +1428,7 @@ int sclbm_autotune(sclbm_sim *s, int trial_steps, sclbm_tuning *best, double *be
         s->chunk_override = saved_chunk;
         s->staging = saved_stg;
         s->tile = saved_tile;
+        s->item_order = saved_order;
         plan_fused(s);
         return rc;
     }
@@ -1416,6 +1436,7 @@ int sclbm_autotune(sclbm_sim *s, int trial_steps, sclbm_tuning *best, double *be
     s->chunk_override = win.chunk;
     s->staging = win.staging;
     s->tile = win.tile;
+    s->item_order = win.order;
     plan_fused(s);
     for (auto &g : s->graph)
         if (g) cudaGraphExecDestroy(g), g = nullptr;

@@ -38,7 +38,7 @@ _STATUS = {OK: 'ok', ERR_ARG: 'invalid argument', ERR_UNSUPPORTED: 'unsupported 
 
 class Tuning(ctypes.Structure):
     _fields_ = [('path', ctypes.c_int), ('chunk', ctypes.c_int), ('staging', ctypes.c_int), ('tile', ctypes.c_int),
-                ('grid', ctypes.c_int)]
+                ('order', ctypes.c_int), ('grid', ctypes.c_int)]
 
 
 class Params(ctypes.Structure):
@@ -321,22 +321,22 @@ class Sim:
         call('sclbm_get_tuning', self.h, ctypes.byref(p), ctypes.byref(c), ctypes.byref(g))
         return p.value, c.value, g.value
 
-    def set_tuning_ex(self, path=PATH_AUTO, chunk=0, staging=STAGE_AUTO, tile=-1):
-        t = Tuning(int(path), int(chunk), int(staging), int(tile), 0)
+    def set_tuning_ex(self, path=PATH_AUTO, chunk=0, staging=STAGE_AUTO, tile=-1, order=-1):
+        t = Tuning(int(path), int(chunk), int(staging), int(tile), int(order), 0)
         call('sclbm_set_tuning_ex', self.h, ctypes.byref(t))
 
     def get_tuning_ex(self):
-        """dict(path, chunk, staging, tile, grid) of what runs"""
+        """dict(path, chunk, staging, tile, order, grid) of what runs"""
         t = Tuning()
         call('sclbm_get_tuning_ex', self.h, ctypes.byref(t))
-        return dict(path=t.path, chunk=t.chunk, staging=t.staging, tile=t.tile, grid=t.grid)
+        return dict(path=t.path, chunk=t.chunk, staging=t.staging, tile=t.tile, order=t.order, grid=t.grid)
 
     def autotune(self, trial_steps=20):
         """Time the bit-identical variants of this handle's step, apply and
         cache the fastest; returns (dict of the configuration, ms per step)."""
         t, ms = Tuning(), ctypes.c_double()
         call('sclbm_autotune', self.h, int(trial_steps), ctypes.byref(t), ctypes.byref(ms))
-        return dict(path=t.path, chunk=t.chunk, staging=t.staging, tile=t.tile, grid=t.grid), ms.value
+        return dict(path=t.path, chunk=t.chunk, staging=t.staging, tile=t.tile, order=t.order, grid=t.grid), ms.value
 
     def info(self):
         v, b = ctypes.c_int64(), ctypes.c_int64()

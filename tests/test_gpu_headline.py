@@ -150,22 +150,24 @@ def test_cfg2_shape_fp32_single_pass_vs_reference(staging):
 
 
 def test_fp32_staged_variants_bit_identical():
-    """Staging and the tile shape change where loads land and which CTA
-    computes a cell, not the arithmetic: populations are bit-identical for
-    every staging and every tile shape, with partial tiles in x and y, a short
+    """Staging, the tile shape, streaming stores and the order of the work
+    items change where loads land and which CTA computes a cell, not the
+    arithmetic: populations are bit-identical for every variant, with partial
+    tiles in x and y, a short
     last chunk, and Lx = 36 (not a multiple of 32; TMA boxes run past the edge
     and are zero-filled there)."""
     x, f = XIStencils['D3Q19'], FStencils['D3E8']
-    variants = [(stg, 0) for stg in (0, 1, 2, 3)] + [(0, tile) for tile in (1, 2, 3)]
+    variants = [(stg, 0, 0) for stg in (0, 1, 2, 3)] + [(0, tile, 0) for tile in (1, 2, 3, 4)] + \
+        [(0, 0, order) for order in (1, 2)]
     for dims in [(36, 20, 23), (64, 24, 16)]:
         n0 = droplet(dims, 5.0, 4.6, 0.16, 2.0, 17)
         pops = []
-        for stg, tile in variants:
+        for stg, tile, order in variants:
             s = _lib.Sim(3, dims, x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], -4.5, tau=0.9,
                          precision=_lib.FP32_SHIFTED, rho0=0.16)
-            s.set_tuning_ex(_lib.PATH_AUTO, 6, stg, tile)
+            s.set_tuning_ex(_lib.PATH_AUTO, 6, stg, tile, order)
             t = s.get_tuning_ex()
-            assert t['staging'] == stg and t['tile'] == tile
+            assert t['staging'] == stg and t['tile'] == tile and t['order'] == order
             s.set_density(n0)
             s.set_velocity(np.zeros(3 * s.V))
             s.init_populations()
