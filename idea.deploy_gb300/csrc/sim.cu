@@ -589,7 +589,10 @@ void plan_fused(sclbm_sim *s) {
         g.tiles_x = (s->L[0] + kTiles[g.tile].tx - 1) / kTiles[g.tile].tx;
         g.tiles_y = (s->L[1] + kTiles[g.tile].ty - 1) / kTiles[g.tile].ty;
     }
-    g.order = (s->item_order > 0 && s->item_order <= 2 && !s->walls && !s->noise_kind && !g.stg) ? s->item_order : 0;
+    // work-item order (k_fused only; y fastest exists in 3D only)
+    g.order = (s->item_order > 0 && s->item_order <= (s->D == 3 ? 2 : 1) && !s->walls && !s->noise_kind && !g.stg)
+                  ? s->item_order
+                  : 0;
     const int resident = s->sms * (s->noise_kind ? o->fused_noise_occupancy()
                                    : s->walls    ? o->fused_walls_occupancy()
                                                  : o->fused_occupancy(g.pairs, g.stg, g.tile));

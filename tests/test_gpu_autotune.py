@@ -40,7 +40,7 @@ def test_autotune_picks_a_bit_identical_variant(dims, st):
     assert cfg['staging'] in (0, 1, 2, 3) and cfg['tile'] in (0, 1, 2, 3, 4) and cfg['order'] in (0, 1, 2)
     assert cfg['staging'] == 0 or cfg['tile'] == 0
     if len(dims) == 2:
-        assert cfg['path'] == _lib.PATH_FUSED and cfg['staging'] == 0 and cfg['tile'] == 0 and cfg['order'] == 0
+        assert cfg['path'] == _lib.PATH_FUSED and cfg['staging'] == 0 and cfg['tile'] == 0 and cfg['order'] in (0, 1)
     assert np.array_equal(a.get_populations(), before)      # trials leave the state as it was
     _lib.clear_tuning_cache()
     b = _sim(dims, st)                                      # the planner's default variant
