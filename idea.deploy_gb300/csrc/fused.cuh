@@ -45,11 +45,18 @@ enum : int { STG_HALO_ASYNC = 1, STG_OWN_TMA = 2 };
 // Shape 4 is the default shape with streaming stores (st.global.cs: the
 // pushed populations are not read again within the step, so they are marked
 // evict-first and leave L2 to the halo lines that neighbouring tiles re-read).
+// Shape 5 is the default shape with the per-plane __syncthreads replaced by
+// an mbarrier per psi-ring slot: a thread arrives once it has written its psi
+// values of a plane and waits only for the slot it is about to read, so warps
+// may drift apart by up to two planes instead of meeting at every plane (the
+// ring holds 2R+4 planes so that a slot is rewritten only after the slowest
+// warp has left it).  The waits are bounded (an error flag for the host).
 struct TileShape {
-    int tx, ty, minb, cs;
+    int tx, ty, minb, cs, mb;
 };
-constexpr TileShape kTiles[] = {{32, 8, 4, 0}, {64, 8, 2, 0}, {32, 16, 2, 0}, {128, 8, 1, 0}, {32, 8, 4, 1}};
-constexpr int N_TILES = 5;
+constexpr TileShape kTiles[] = {{32, 8, 4, 0, 0}, {64, 8, 2, 0, 0}, {32, 16, 2, 0, 0},
+                                {128, 8, 1, 0, 0}, {32, 8, 4, 1, 0}, {32, 8, 4, 0, 1}};
+constexpr int N_TILES = 6;
 
 template <class L, class S, int TXp = 0, int TYp = 0>
 struct FusedShape {
@@ -83,6 +90,9 @@ struct FusedShape {
     static constexpr int own_offset(int stg) {
         return ((RING_BYTES + ((stg & STG_HALO_ASYNC) ? HALO_BYTES : 0)) + 127) / 128 * 128;
     }
+    // the mbarrier-ring variant: 2R+4 psi planes and one mbarrier per slot
+    static constexpr int MB_RING = 2 * R + 4;
+    static constexpr int MB_SMEM = MB_RING * HC * 4 + MB_RING * 8;
     static constexpr int stg_smem(int stg) {
         return (stg & STG_OWN_TMA) ? own_offset(stg) + 2 * OWN_BOX_BYTES + 16
                                    : RING_BYTES + ((stg & STG_HALO_ASYNC) ? HALO_BYTES : 0);
@@ -98,6 +108,12 @@ __device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
     asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
 }
 __device__ __forceinline__ void mbar_fence_init() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
+__device__ __forceinline__ void mbar_inval(uint64_t *bar) {
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];\n" ::"r"(smem_u32(bar)) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
+}
 __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
                  : "memory");
@@ -258,7 +274,7 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
 // step; the batched sweeps use it (their Laplace-pressure criterion sees that
 // drift on large droplets).  The density used by the physics is unchanged.
 template <class L, class S, bool MRT, class ST = void, bool WALLS = false, bool PAIRS = false, int STG = 0,
-          int TXT = 0, int TYT = 0, bool EXACT_REST = false, bool CS = false>
+          int TXT = 0, int TYT = 0, bool EXACT_REST = false, bool CS = false, bool MB = false>
 __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float *__restrict__ pop_out, const int V,
                                            const int Lx, const int Ly, const int Lz, const int x0, const int y0,
                                            const int m0, const int m1, const float neg_g, const float rho0,
@@ -274,7 +290,10 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
     constexpr bool HALO_ASYNC = (STG & STG_HALO_ASYNC) != 0, OWN_TMA = (STG & STG_OWN_TMA) != 0;
     using SeedT = typename std::conditional<NOISE, ST, int>::type;
     using SH = FusedShape<L, S, TXT, TYT>;
-    constexpr int D = L::D, Q = L::Q, R = SH::R, HX = SH::HX, HC = SH::HC, NT = SH::NT, RING = SH::RING;
+    constexpr int D = L::D, Q = L::Q, R = SH::R, HX = SH::HX, HC = SH::HC, NT = SH::NT;
+    constexpr int RING = MB ? SH::MB_RING : SH::RING;
+    static_assert(!MB || (PAIRS && STG == 0 && !WALLS && std::is_void<ST>::value && D == 3), "mbarrier ring");
+    uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + RING * HC);  // MB: one per ring slot
     float *ring = smem;  // psi ring [RING][HC], then (2D) 2 stage buffers [HPT][Q][NT]
     float *stage0 = smem + RING * HC;
     unsigned char *fring = reinterpret_cast<unsigned char *>(smem + RING * HC + 2 * SH::STAGE);  // WALLS
@@ -455,10 +474,23 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
     // loads are in flight together
     constexpr bool STAGED = D == 2;
     __syncthreads();  // the previous item's readers are done with the ring (and the own buffers)
+    if constexpr (MB) {
+        // fresh phases for this item: every arrival of the previous item completed its phase
+        if (tid == 0)
+            for (int k = 0; k < RING; k++) {
+                mbar_inval(&mbar[k]);
+                mbar_init(&mbar[k], NT);
+            }
+        __syncthreads();
+    }
     own_issue(m0);
     for (int m = m0 - R; m < m0 + R; m++) psi_plane(m);
     if (STAGED) stage_issue(m0 + R);
     halo_issue(m0 + R);
+    if constexpr (MB) {
+        psi_plane(m0 + R);  // one plane ahead; the main loop computes m+R+1
+        __syncthreads();
+    }
     for (int m = m0; m < m1; m++) {
         int Z3[3];
 #pragma unroll
@@ -485,10 +517,21 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
         } else if (HALO_ASYNC) {
             halo_reduce(m + R);
             if (m + 1 < m1) halo_issue(m + R + 1);
+        } else if (MB) {
+            if (m + 1 < m1) {
+                psi_plane(m + R + 1);
+                mbar_arrive(&mbar[wrapm(m + R + 1, RING)]);
+            }
         } else {
             psi_plane(m + R);
         }
-        __syncthreads();
+        if constexpr (MB) {
+            // plane m+R was written in the previous iteration (or the preamble);
+            // its slot's k-th main-loop use has phase k & 1
+            if (m > m0) mbar_wait_bounded(&mbar[wrapm(m + R, RING)], ((m - m0 - 1) / RING) & 1, err, *dead);
+        } else {
+            __syncthreads();
+        }
         if constexpr (OWN_TMA) {
             // buffer of plane m+1 was last read for plane m-1, before the barrier
             if (m + 1 < m1) own_issue(m + 1);
@@ -629,10 +672,19 @@ __global__ void __launch_bounds__(TILE ? kTiles[TILE].tx * kTiles[TILE].ty : Fus
     k_fused(const float *__restrict__ pop, float *__restrict__ pop_out, const __grid_constant__ StepParams<L, S, float> p,
             const FusedGeom fg) {
     constexpr int TXT = TILE ? kTiles[TILE].tx : 0, TYT = TILE ? kTiles[TILE].ty : 0;
+    constexpr bool MB = kTiles[TILE].mb != 0;
     using SH = FusedShape<L, S, TXT, TYT>;
     constexpr int D = L::D;
     extern __shared__ float smem[];
     const int Lm = D == 3 ? fg.L[2] : fg.L[1];
+    bool dead = false;
+    if constexpr (MB) {
+        // initialised once here; each item re-initialises them (fused_tile)
+        uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + SH::MB_RING * SH::HC);
+        if (threadIdx.x == 0)
+            for (int k = 0; k < SH::MB_RING; k++) mbar_init(&mbar[k], SH::NT);
+        __syncthreads();
+    }
     for (int item = blockIdx.x; item < fg.items; item += gridDim.x) {
         // order of the work items over the grid: 0 x fastest, then y, then
         // the chunk; 1 the chunk fastest (a tile column's chunks together);
@@ -655,9 +707,10 @@ __global__ void __launch_bounds__(TILE ? kTiles[TILE].tx * kTiles[TILE].ty : Fus
             ic = D == 3 ? rest / fg.tiles_y : rest;
         }
         const int m0 = ic * fg.chunk;
-        fused_tile<L, S, MRT, void, false, PAIRS, 0, TXT, TYT, false, kTiles[TILE].cs != 0>(
+        fused_tile<L, S, MRT, void, false, PAIRS, 0, TXT, TYT, false, kTiles[TILE].cs != 0, MB>(
             pop, pop_out, (int)fg.V, fg.L[0], fg.L[1], fg.L[2], ix * SH::TX, iy * SH::TY, m0, min(m0 + fg.chunk, Lm),
-            p.neg_g, p.rho0, p, smem);
+            p.neg_g, p.rho0, p, smem, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, fg.err,
+            &dead);
     }
 }
 

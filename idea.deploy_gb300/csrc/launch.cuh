@@ -197,14 +197,18 @@ struct Ops {
     static constexpr int STG_MASK = STG_BUILT ? 3 : 0;
     static constexpr int TILE_MASK = STG_BUILT ? (1 << N_TILES) - 1 : 1;
     template <int TILE>
-    static void allow_tile_smem() {
+    static constexpr int tile_smem() {
         using SH = FusedShape<L, S, kTiles[TILE].tx, kTiles[TILE].ty>;
+        return kTiles[TILE].mb ? SH::MB_SMEM : SH::SMEM;
+    }
+    template <int TILE>
+    static void allow_tile_smem() {
         static bool done[64] = {};
         int dev = 0;
         cudaGetDevice(&dev);
         if (dev < 0 || dev >= 64 || !done[dev]) {
             cudaFuncSetAttribute(k_fused<L, S, MRT, true, TILE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 SH::SMEM);
+                                 tile_smem<TILE>());
             if (dev >= 0 && dev < 64) done[dev] = true;
         }
     }
@@ -213,8 +217,8 @@ struct Ops {
                                    cudaStream_t st) {
         using SH = FusedShape<L, S, kTiles[TILE].tx, kTiles[TILE].ty>;
         allow_tile_smem<TILE>();
-        k_fused<L, S, MRT, true, TILE><<<grid, SH::NT, SH::SMEM, st>>>((const float *)pop, (float *)pop_out,
-                                                                      *static_cast<const SP *>(sp), fg);
+        k_fused<L, S, MRT, true, TILE><<<grid, SH::NT, tile_smem<TILE>(), st>>>(
+            (const float *)pop, (float *)pop_out, *static_cast<const SP *>(sp), fg);
         return cudaGetLastError();
     }
     template <int TILE>
@@ -222,7 +226,7 @@ struct Ops {
         using SH = FusedShape<L, S, kTiles[TILE].tx, kTiles[TILE].ty>;
         allow_tile_smem<TILE>();
         int b = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fused<L, S, MRT, true, TILE>, SH::NT, SH::SMEM);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fused<L, S, MRT, true, TILE>, SH::NT, tile_smem<TILE>());
         return b > 0 ? b : 1;
     }
     template <int STG>
@@ -258,6 +262,7 @@ struct Ops {
                 if (fg.pairs && !fg.stg && fg.tile == 2) return launch_tile<2>(pop, pop_out, sp, fg, grid, st);
                 if (fg.pairs && !fg.stg && fg.tile == 3) return launch_tile<3>(pop, pop_out, sp, fg, grid, st);
                 if (fg.pairs && !fg.stg && fg.tile == 4) return launch_tile<4>(pop, pop_out, sp, fg, grid, st);
+                if (fg.pairs && !fg.stg && fg.tile == 5) return launch_tile<5>(pop, pop_out, sp, fg, grid, st);
             }
             if (fg.stg || fg.tile) return cudaErrorNotSupported;
             if constexpr (L::D == 3 && S::R % 2 == 0) {
@@ -310,6 +315,7 @@ struct Ops {
                 if (pairs && tile == 2) return occupancy_tile<2>();
                 if (pairs && tile == 3) return occupancy_tile<3>();
                 if (pairs && tile == 4) return occupancy_tile<4>();
+                if (pairs && tile == 5) return occupancy_tile<5>();
             }
             int b = 0;
             if constexpr (L::D == 3 && S::R % 2 == 0) {
