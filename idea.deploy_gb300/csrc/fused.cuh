@@ -75,8 +75,9 @@ struct FusedShape {
     // floats of one plane's staged halo populations (2D only: see k_fused)
     static constexpr int STAGE = D == 2 ? HPT * L::Q * NT : 0;
     static constexpr int SMEM = (RING * HC + 2 * STAGE) * 4;  // psi ring + double-buffered stage
-    // fluctuating step: plus each thread's random moments of its current cell
-    static constexpr int NSMEM = SMEM + (L::Q - D - 1) * NT * 4;
+    // fluctuating step: plus each thread's noise of its current cell's Q - 1
+    // moving populations
+    static constexpr int NSMEM = SMEM + (L::Q - 1) * NT * 4;
     // walls: plus a ring of the halo planes' wall flags (bytes)
     static constexpr int WSMEM = SMEM + (RING * HC + 3) / 4 * 4;
     // staged variants (3D): halo-pair slots [Q][HSTR] float2, then two own
@@ -274,7 +275,7 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
 // step; the batched sweeps use it (their Laplace-pressure criterion sees that
 // drift on large droplets).  The density used by the physics is unchanged.
 template <class L, class S, bool MRT, class ST = void, bool WALLS = false, bool PAIRS = false, int STG = 0,
-          int TXT = 0, int TYT = 0, bool EXACT_REST = false, bool CS = false, bool MB = false>
+          int TXT = 0, int TYT = 0, bool EXACT_REST = false, bool CS = false, bool MB = false, int CRNG = 0>
 __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float *__restrict__ pop_out, const int V,
                                            const int Lx, const int Ly, const int Lz, const int x0, const int y0,
                                            const int m0, const int m1, const float neg_g, const float rho0,
@@ -558,15 +559,18 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
                     fb[o] = fring + wrapm(m + o - 1, RING) * HC + ty * HX + tx + (D == 3 ? R * HX : 0) + R;
                 fluid = fb[1][0] == 1;
             }
-            // random moments of the cell into this thread's shared-memory slot
-            // (the states die here; the collision reads the moments back)
-            float *rms = smem + SH::RING * SH::HC + 2 * SH::STAGE + tid;
+            // the cell's noise per moving population into this thread's
+            // shared-memory slots (the states and moments die here; the
+            // collision adds its population's noise back with one load)
+            float *nzs = smem + SH::RING * SH::HC + 2 * SH::STAGE + tid;
             if constexpr (NOISE) {
                 float rm[NR];
-                noise_compute<L, float, false, SeedT>(*z, 0, st, rm);
+                noise_compute<L, float, false, SeedT, CRNG>(*z, 0, st, rm);
                 noise_store<L, SeedT, int>(0, seeds, (int64_t)V, (int64_t)g, st);
 #pragma unroll
-                for (int k = 0; k < NR; k++) rms[k * NT] = rm[k];
+                for (int q = 1; q < Q; q++)
+                    nzs[(q - 1) * NT] = noise_sum_masked<NR>(NoiseMask<L>::m(q), z->coef[q], rm,
+                                                             std::make_integer_sequence<int, NR>{});
             }
             if (!fluid) {
 #pragma unroll
@@ -629,9 +633,7 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
                                                                   pend[opposite_q<L>(q)]);
                     else out = pend[q];
                 }
-                if constexpr (NOISE)
-                    add_noise_terms_strided<NR, NT>(NoiseMask<L>::m(q), z->coef[q], rms, out,
-                                                    std::make_integer_sequence<int, NR>{});
+                if constexpr (NOISE) out = __fadd_rn(out, nzs[(q - 1) * NT]);
                 // __fsub_rn: no contraction with the product that made `out`
                 // (at omega = 1 it is a plain multiply), so the rest population
                 // balances exactly the rounded values that are stored
@@ -777,7 +779,11 @@ __global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
     }
 }
 
-template <class L, class S, class ST, bool PAIRS = false>
+// CRNG: the generator (CRNG_*), a compile-time constant; ST its state type.
+// Two CTAs per SM (128 registers, no spills): three (80 registers) spill and
+// run no faster at 256^3 (MINSTD 1.318 / 1.327 ms, MMIX 1.465 / 1.472 ms)
+template <class L, class S, int CRNG, bool PAIRS = false,
+          class ST = typename std::conditional<CRNG == CRNG_MMIX, unsigned long long, unsigned int>::type>
 __global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
     k_fused_noise(const float *__restrict__ pop, float *__restrict__ pop_out,
                   const __grid_constant__ StepParams<L, S, float> p, const FusedGeom fg, ST *__restrict__ seeds,
@@ -792,9 +798,9 @@ __global__ void __launch_bounds__(FusedShape<L, S>::NT, 2)
         const int iy = D == 3 ? rest % fg.tiles_y : 0;
         const int ic = D == 3 ? rest / fg.tiles_y : rest;
         const int m0 = ic * fg.chunk;
-        fused_tile<L, S, false, ST, false, PAIRS>(pop, pop_out, (int)fg.V, fg.L[0], fg.L[1], fg.L[2], ix * SH::TX,
-                                                  iy * SH::TY, m0, min(m0 + fg.chunk, Lm), p.neg_g, p.rho0, p, smem,
-                                                  seeds, &z);
+        fused_tile<L, S, false, ST, false, PAIRS, 0, 0, 0, false, false, false, CRNG>(
+            pop, pop_out, (int)fg.V, fg.L[0], fg.L[1], fg.L[2], ix * SH::TX, iy * SH::TY, m0,
+            min(m0 + fg.chunk, Lm), p.neg_g, p.rho0, p, smem, seeds, &z);
     }
 }
 

@@ -85,7 +85,7 @@ struct KernelOps {
     // single-pass fluctuating step (FP32 BGK only, else null)
     cudaError_t (*fused_noise)(const void *pop, void *pop_out, const void *step_params, const FusedGeom &fg,
                                void *seeds, const void *noise_params, int grid, cudaStream_t st);
-    int (*fused_noise_occupancy)();
+    int (*fused_noise_occupancy)(int kind);  // kind: CRNG_*
     unsigned (*noise_mask)(int q);  // nonzero pattern the single-pass noise kernel assumes
     // single-pass step with walls (FP32 BGK only, else null)
     cudaError_t (*fused_walls)(const void *pop, void *pop_out, const void *step_params, const FusedGeom &fg,
@@ -429,35 +429,43 @@ struct Ops {
         }
         return cudaErrorNotSupported;
     }
+    template <int CRNG, bool PAIRS>
+    static cudaError_t launch_noise(const void *pop, void *pop_out, const void *sp, const FusedGeom &fg, void *seeds,
+                                    const NP &z, int grid, cudaStream_t st) {
+        using SH = FusedShape<L, S>;
+        using ST = typename std::conditional<CRNG == CRNG_MMIX, unsigned long long, unsigned int>::type;
+        k_fused_noise<L, S, CRNG, PAIRS><<<grid, SH::NT, SH::NSMEM, st>>>(
+            (const float *)pop, (float *)pop_out, *static_cast<const SP *>(sp), fg, (ST *)seeds, z);
+        return cudaGetLastError();
+    }
+    template <bool PAIRS>
+    static cudaError_t launch_noise_kind(const void *pop, void *pop_out, const void *sp, const FusedGeom &fg,
+                                         void *seeds, const NP &z, int grid, cudaStream_t st) {
+        switch (z.kind) {
+        case CRNG_MINSTD: return launch_noise<CRNG_MINSTD, PAIRS>(pop, pop_out, sp, fg, seeds, z, grid, st);
+        case CRNG_NUMREC: return launch_noise<CRNG_NUMREC, PAIRS>(pop, pop_out, sp, fg, seeds, z, grid, st);
+        case CRNG_MMIX: return launch_noise<CRNG_MMIX, PAIRS>(pop, pop_out, sp, fg, seeds, z, grid, st);
+        default: return cudaErrorInvalidValue;
+        }
+    }
     static cudaError_t fused_noise(const void *pop, void *pop_out, const void *sp, const FusedGeom &fg, void *seeds,
                                    const void *np, int grid, cudaStream_t st) {
         if constexpr (std::is_same<Real, float>::value && !MRT) {
-            using SH = FusedShape<L, S>;
             allow_smem_noise();
             const NP &z = *static_cast<const NP *>(np);
             if constexpr (L::D == 3 && S::R % 2 == 0) {
-                if (fg.pairs) {
-                    if (z.kind == CRNG_MMIX)
-                        k_fused_noise<L, S, unsigned long long, true><<<grid, SH::NT, SH::NSMEM, st>>>(
-                            (const float *)pop, (float *)pop_out, *static_cast<const SP *>(sp), fg,
-                            (unsigned long long *)seeds, z);
-                    else
-                        k_fused_noise<L, S, unsigned int, true><<<grid, SH::NT, SH::NSMEM, st>>>(
-                            (const float *)pop, (float *)pop_out, *static_cast<const SP *>(sp), fg,
-                            (unsigned int *)seeds, z);
-                    return cudaGetLastError();
-                }
+                if (fg.pairs) return launch_noise_kind<true>(pop, pop_out, sp, fg, seeds, z, grid, st);
             }
-            if (z.kind == CRNG_MMIX)
-                k_fused_noise<L, S, unsigned long long><<<grid, SH::NT, SH::NSMEM, st>>>(
-                    (const float *)pop, (float *)pop_out, *static_cast<const SP *>(sp), fg, (unsigned long long *)seeds,
-                    z);
-            else
-                k_fused_noise<L, S, unsigned int><<<grid, SH::NT, SH::NSMEM, st>>>(
-                    (const float *)pop, (float *)pop_out, *static_cast<const SP *>(sp), fg, (unsigned int *)seeds, z);
-            return cudaGetLastError();
+            return launch_noise_kind<false>(pop, pop_out, sp, fg, seeds, z, grid, st);
         }
         return cudaErrorNotSupported;
+    }
+    template <bool PAIRS>
+    static void allow_smem_noise_pairs() {
+        constexpr int n = FusedShape<L, S>::NSMEM;
+        cudaFuncSetAttribute(k_fused_noise<L, S, CRNG_MINSTD, PAIRS>, cudaFuncAttributeMaxDynamicSharedMemorySize, n);
+        cudaFuncSetAttribute(k_fused_noise<L, S, CRNG_NUMREC, PAIRS>, cudaFuncAttributeMaxDynamicSharedMemorySize, n);
+        cudaFuncSetAttribute(k_fused_noise<L, S, CRNG_MMIX, PAIRS>, cudaFuncAttributeMaxDynamicSharedMemorySize, n);
     }
     static void allow_smem_noise() {
         if constexpr (std::is_same<Real, float>::value && !MRT) {
@@ -465,27 +473,23 @@ struct Ops {
             int dev = 0;
             cudaGetDevice(&dev);
             if (dev < 0 || dev >= 64 || !done[dev]) {
-                cudaFuncSetAttribute(k_fused_noise<L, S, unsigned int>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     FusedShape<L, S>::NSMEM);
-                cudaFuncSetAttribute(k_fused_noise<L, S, unsigned long long>,
-                                     cudaFuncAttributeMaxDynamicSharedMemorySize, FusedShape<L, S>::NSMEM);
-                if constexpr (L::D == 3 && S::R % 2 == 0) {
-                    cudaFuncSetAttribute(k_fused_noise<L, S, unsigned int, true>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, FusedShape<L, S>::NSMEM);
-                    cudaFuncSetAttribute(k_fused_noise<L, S, unsigned long long, true>,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, FusedShape<L, S>::NSMEM);
-                }
+                allow_smem_noise_pairs<false>();
+                if constexpr (L::D == 3 && S::R % 2 == 0) allow_smem_noise_pairs<true>();
                 if (dev >= 0 && dev < 64) done[dev] = true;
             }
         }
     }
-    static int fused_noise_occupancy() {
+    static int fused_noise_occupancy(int kind) {
         int b = 0;
         if constexpr (std::is_same<Real, float>::value && !MRT) {
             using SH = FusedShape<L, S>;
             allow_smem_noise();
-            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fused_noise<L, S, unsigned long long>, SH::NT,
-                                                          SH::NSMEM);
+            if (kind == CRNG_MINSTD)
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fused_noise<L, S, CRNG_MINSTD>, SH::NT, SH::NSMEM);
+            else if (kind == CRNG_NUMREC)
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fused_noise<L, S, CRNG_NUMREC>, SH::NT, SH::NSMEM);
+            else
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fused_noise<L, S, CRNG_MMIX>, SH::NT, SH::NSMEM);
         }
         return b > 0 ? b : 1;
     }

@@ -179,27 +179,30 @@ __device__ __forceinline__ T nonzero_state(T a) {
     return a == 0 ? T(1) : a;
 }
 
-// advance the states and form the random moments
-template <class L, class Real, bool STRICT, class T>
+// advance the states and form the random moments.  KIND (a CRNG_* value, or 0
+// for z.kind at run time): with the generator known at compile time only its
+// own update and conversion are emitted, not the three generators' selected
+template <class L, class Real, bool STRICT, class T, int KIND = 0>
 __device__ __forceinline__ void noise_compute(const NoiseParams<L, Real> &z, int indep, T *st, Real *rm) {
     constexpr int NR = NoiseParams<L, Real>::NR;
+    const int kind = KIND ? KIND : z.kind;
     if (indep) {
 #pragma unroll
         for (int k = 0; k < NR; k++) {
-            const T a = (T)crng_next(z.kind, st[2 * k]), b = (T)crng_next(z.kind, st[2 * k + 1]);
+            const T a = (T)crng_next(kind, st[2 * k]), b = (T)crng_next(kind, st[2 * k + 1]);
             st[2 * k] = a;
             st[2 * k + 1] = b;
-            rm[k] = box_muller<Real, STRICT>(z.m2var[k], crng_uniform<Real, STRICT>(z.kind, nonzero_state(a)),
-                                             crng_uniform<Real, STRICT>(z.kind, b));
+            rm[k] = box_muller<Real, STRICT>(z.m2var[k], crng_uniform<Real, STRICT>(kind, nonzero_state(a)),
+                                             crng_uniform<Real, STRICT>(kind, b));
         }
     } else {
 #pragma unroll
         for (int k = 0; k < NR; k++) {
-            const T a = (T)crng_next(z.kind, st[k]);
-            const T b = (T)crng_next(z.kind, a);
+            const T a = (T)crng_next(kind, st[k]);
+            const T b = (T)crng_next(kind, a);
             st[k] = b;
-            rm[k] = box_muller<Real, STRICT>(z.m2var[k], crng_uniform<Real, STRICT>(z.kind, nonzero_state(a)),
-                                             crng_uniform<Real, STRICT>(z.kind, b));
+            rm[k] = box_muller<Real, STRICT>(z.m2var[k], crng_uniform<Real, STRICT>(kind, nonzero_state(a)),
+                                             crng_uniform<Real, STRICT>(kind, b));
         }
     }
 }
@@ -217,17 +220,20 @@ __device__ __forceinline__ void add_noise_terms(const Real *coef, const Real *rm
                                                 std::integer_sequence<int, I...>) {
     (add_noise_term<NR, I, Real, STRICT>(coef, rm, acc), ...);
 }
-// FP32 variant reading the moments from a shared-memory slot, rm[k * STRIDE],
-// terms outside the lattice's nonzero pattern skipped (q constant after unrolling)
-template <int NR, int STRIDE, int I>
-__device__ __forceinline__ void add_noise_term_masked(unsigned mask, const float *coef, const float *rm, float &acc) {
+// FP32 single pass: the noise of one population, sum_k coef[k] Rm_k from the
+// moments in registers, terms outside the lattice's nonzero pattern skipped
+// (mask a constant after unrolling), in the reference's print order
+template <int NR, int I>
+__device__ __forceinline__ void noise_term_masked(unsigned mask, const float *coef, const float *rm, float &acc) {
     constexpr int k = name_order<NR>(I);
-    if ((mask >> k) & 1u) acc = fmaf(coef[k], rm[k * STRIDE], acc);
+    if ((mask >> k) & 1u) acc = fmaf(coef[k], rm[k], acc);
 }
-template <int NR, int STRIDE, int... I>
-__device__ __forceinline__ void add_noise_terms_strided(unsigned mask, const float *coef, const float *rm, float &acc,
-                                                        std::integer_sequence<int, I...>) {
-    (add_noise_term_masked<NR, STRIDE, I>(mask, coef, rm, acc), ...);
+template <int NR, int... I>
+__device__ __forceinline__ float noise_sum_masked(unsigned mask, const float *coef, const float *rm,
+                                                  std::integer_sequence<int, I...>) {
+    float acc = 0.f;
+    (noise_term_masked<NR, I>(mask, coef, rm, acc), ...);
+    return acc;
 }
 template <class L, class Real, bool STRICT>
 __device__ __forceinline__ void add_noise(const NoiseParams<L, Real> &z, const Real *rm, Real *out) {

@@ -593,7 +593,7 @@ void plan_fused(sclbm_sim *s) {
     g.order = (s->item_order > 0 && s->item_order <= (s->D == 3 ? 2 : 1) && !s->walls && !s->noise_kind && !g.stg)
                   ? s->item_order
                   : 0;
-    const int resident = s->sms * (s->noise_kind ? o->fused_noise_occupancy()
+    const int resident = s->sms * (s->noise_kind ? o->fused_noise_occupancy(s->noise_kind)
                                    : s->walls    ? o->fused_walls_occupancy()
                                                  : o->fused_occupancy(g.pairs, g.stg, g.tile));
     const int base = g.tiles_x * g.tiles_y;
