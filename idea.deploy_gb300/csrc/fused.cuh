@@ -485,7 +485,24 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
         __syncthreads();
     }
     own_issue(m0);
-    for (int m = m0 - R; m < m0 + R; m++) psi_plane(m);
+    if constexpr (STAGED) {
+        // 2D: the preamble's planes through the two stage buffers, the next
+        // plane's copy in flight while this one is reduced (each thread reads
+        // back only its own copies, so no barrier between a reduce and the
+        // copy that reuses the buffer); same sums as psi_plane
+        stage_issue(m0 - R);
+        for (int m = m0 - R; m < m0 + R; m++) {
+            if (m + 1 < m0 + R) {
+                stage_issue(m + 1);
+                cp_async_wait<1>();
+            } else {
+                cp_async_wait<0>();
+            }
+            stage_reduce(m);
+        }
+    } else {
+        for (int m = m0 - R; m < m0 + R; m++) psi_plane(m);
+    }
     if (STAGED) stage_issue(m0 + R);
     halo_issue(m0 + R);
     if constexpr (MB) {
