@@ -1858,7 +1858,9 @@ struct sclbm_batch {
 namespace {
 
 constexpr int BATCH_CHUNK = 32;     // longest run of planes per work item
-constexpr int BATCH_MIN_CHUNK = 4;  // shortest (items are re-planned as lattices retire)
+// shortest (items are re-planned as lattices retire): 2 rather than 4 took
+// the step of a lone 224^2 D2Q9 E8 droplet from 8.3 to 6.3 us
+constexpr int BATCH_MIN_CHUNK = 2;
 constexpr int BATCH_CHECK_BLOCKS = 32;  // blocks per lattice in the observable kernels
 
 int balloc(sclbm_batch *b, void **p, size_t bytes) {
