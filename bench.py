@@ -475,7 +475,7 @@ def run_ours(a, dist):
                       'chunk_planes': chunk, 'grid': grid,
                       'tuned': dict(tuned, trial_ms_per_step=tuned_ms,
                                     tile_shape=['32x8', '64x8', '32x16', '128x8', '32x8, streaming stores',
-                                                '32x8, mbarrier psi planes', '32x8, L2 prefetch'][tuned.get('tile', 0)],
+                                                '32x8, mbarrier psi planes'][tuned.get('tile', 0)],
                                     by='sclbm_autotune (%d trial launches per candidate)' % a.tune_steps),
                       'collision_kernel': 'MRT with all rates 1.0 is exactly BGK with omega=1: sparse BGK operator'},
         'roofline': {'bound': 'hbm', 'kernel': 'k_fused (single pass)' if path in (2, 3) else

@@ -51,16 +51,12 @@ enum : int { STG_HALO_ASYNC = 1, STG_OWN_TMA = 2 };
 // may drift apart by up to two planes instead of meeting at every plane (the
 // ring holds 2R+4 planes so that a slot is rewritten only after the slowest
 // warp has left it).  The waits are bounded (an error flag for the host).
-// Shape 6 is the default shape that also prefetches into L2 the tile's own
-// rows of the plane pf planes ahead of its psi reduction (prefetch.global.L2:
-// more lines in flight without registers, shared memory or waits).
 struct TileShape {
-    int tx, ty, minb, cs, mb, pf;
+    int tx, ty, minb, cs, mb;
 };
-constexpr TileShape kTiles[] = {{32, 8, 4, 0, 0, 0}, {64, 8, 2, 0, 0, 0}, {32, 16, 2, 0, 0, 0},
-                                {128, 8, 1, 0, 0, 0}, {32, 8, 4, 1, 0, 0}, {32, 8, 4, 0, 1, 0},
-                                {32, 8, 4, 0, 0, 2}};
-constexpr int N_TILES = 7;
+constexpr TileShape kTiles[] = {{32, 8, 4, 0, 0}, {64, 8, 2, 0, 0}, {32, 16, 2, 0, 0},
+                                {128, 8, 1, 0, 0}, {32, 8, 4, 1, 0}, {32, 8, 4, 0, 1}};
+constexpr int N_TILES = 6;
 
 template <class L, class S, int TXp = 0, int TYp = 0>
 struct FusedShape {
@@ -279,8 +275,7 @@ __device__ __forceinline__ void two_sum(float a, float b, float &s, float &e) {
 // step; the batched sweeps use it (their Laplace-pressure criterion sees that
 // drift on large droplets).  The density used by the physics is unchanged.
 template <class L, class S, bool MRT, class ST = void, bool WALLS = false, bool PAIRS = false, int STG = 0,
-          int TXT = 0, int TYT = 0, bool EXACT_REST = false, bool CS = false, bool MB = false, int CRNG = 0,
-          int PF = 0>
+          int TXT = 0, int TYT = 0, bool EXACT_REST = false, bool CS = false, bool MB = false, int CRNG = 0>
 __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float *__restrict__ pop_out, const int V,
                                            const int Lx, const int Ly, const int Lz, const int x0, const int y0,
                                            const int m0, const int m1, const float neg_g, const float rho0,
@@ -299,8 +294,6 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
     constexpr int D = L::D, Q = L::Q, R = SH::R, HX = SH::HX, HC = SH::HC, NT = SH::NT;
     constexpr int RING = MB ? SH::MB_RING : SH::RING;
     static_assert(!MB || (PAIRS && STG == 0 && !WALLS && std::is_void<ST>::value && D == 3), "mbarrier ring");
-    static_assert(PF == 0 || (PAIRS && STG == 0 && !MB && !WALLS && std::is_void<ST>::value && D == 3),
-                  "L2 prefetch");
     uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + RING * HC);  // MB: one per ring slot
     float *ring = smem;  // psi ring [RING][HC], then (2D) 2 stage buffers [HPT][Q][NT]
     float *stage0 = smem + RING * HC;
@@ -476,25 +469,6 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
         }
     };
 
-    // PF: L2 prefetch of the tile's own rows of plane m (one 128-byte line
-    // per population and row; rows that do not start on a line also get
-    // their last line).  No data comes back to the SM, nothing waits on it:
-    // the psi reduction of plane m, PF planes later, and the neighbouring
-    // tiles' halo loads of that plane then hit L2.
-    auto l2_prefetch = [&](int m) {
-        if constexpr (PF > 0) {
-            if (tid < Q * SH::TY) {
-                const int q = tid / SH::TY, yy = y0 + tid % SH::TY;
-                if (yy < Ly) {
-                    const float *a = pop + (q * V + wrapm(m, Lm) * PL + yy * Lx + x0);
-                    asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
-                    if (((q * V + wrapm(m, Lm) * PL + yy * Lx + x0) & 31) != 0 || Lx - x0 < SH::TX)
-                        asm volatile("prefetch.global.L2 [%0];" ::"l"(a + (min(SH::TX, Lx - x0) - 1)));
-                }
-            }
-        }
-    };
-
     // 2D: the halo of plane m+R+1 is prefetched with cp.async during plane m;
     // 3D: the halo (1.7x the tile) is reduced straight from L2 and the
     // thread's own populations of plane m are loaded first, so both sets of
@@ -527,9 +501,6 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
             stage_reduce(m);
         }
     } else {
-        if constexpr (PF > 0)
-            for (int k = 0; k < PF; k++)
-                if (m0 + k < m1) l2_prefetch(m0 + R + k);
         for (int m = m0 - R; m < m0 + R; m++) psi_plane(m);
     }
     if (STAGED) stage_issue(m0 + R);
@@ -539,8 +510,6 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
         __syncthreads();
     }
     for (int m = m0; m < m1; m++) {
-        if constexpr (PF > 0)
-            if (m + PF < m1) l2_prefetch(m + R + PF);
         int Z3[3];
 #pragma unroll
         for (int o = -1; o <= 1; o++) Z3[o + 1] = D == 3 ? wrapc(m + o, Lm) * PL : wrapc(m + o, Lm) * Lx;
@@ -757,7 +726,7 @@ __global__ void __launch_bounds__(TILE ? kTiles[TILE].tx * kTiles[TILE].ty : Fus
             ic = D == 3 ? rest / fg.tiles_y : rest;
         }
         const int m0 = ic * fg.chunk;
-        fused_tile<L, S, MRT, void, false, PAIRS, 0, TXT, TYT, false, kTiles[TILE].cs != 0, MB, 0, kTiles[TILE].pf>(
+        fused_tile<L, S, MRT, void, false, PAIRS, 0, TXT, TYT, false, kTiles[TILE].cs != 0, MB>(
             pop, pop_out, (int)fg.V, fg.L[0], fg.L[1], fg.L[2], ix * SH::TX, iy * SH::TY, m0, min(m0 + fg.chunk, Lm),
             p.neg_g, p.rho0, p, smem, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, fg.err,
             &dead);

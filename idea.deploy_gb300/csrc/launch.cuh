@@ -263,7 +263,6 @@ struct Ops {
                 if (fg.pairs && !fg.stg && fg.tile == 3) return launch_tile<3>(pop, pop_out, sp, fg, grid, st);
                 if (fg.pairs && !fg.stg && fg.tile == 4) return launch_tile<4>(pop, pop_out, sp, fg, grid, st);
                 if (fg.pairs && !fg.stg && fg.tile == 5) return launch_tile<5>(pop, pop_out, sp, fg, grid, st);
-                if (fg.pairs && !fg.stg && fg.tile == 6) return launch_tile<6>(pop, pop_out, sp, fg, grid, st);
             }
             if (fg.stg || fg.tile) return cudaErrorNotSupported;
             if constexpr (L::D == 3 && S::R % 2 == 0) {
@@ -317,7 +316,6 @@ struct Ops {
                 if (pairs && tile == 3) return occupancy_tile<3>();
                 if (pairs && tile == 4) return occupancy_tile<4>();
                 if (pairs && tile == 5) return occupancy_tile<5>();
-                if (pairs && tile == 6) return occupancy_tile<6>();
             }
             int b = 0;
             if constexpr (L::D == 3 && S::R % 2 == 0) {

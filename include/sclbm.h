@@ -275,8 +275,7 @@ SCLBM_API int sclbm_get_tuning(const sclbm_sim *s, int *path, int *chunk, int *g
  * automatic), tile (tile shape of the 3D paired single pass, FP32 BGK
  * without walls or noise: 0 = 32x8, 1 = 64x8, 2 = 32x16, 3 = 128x8, 4 = 32x8
  * with streaming (evict-first) stores, 5 = 32x8 with an mbarrier per psi
- * plane in place of the per-plane block barrier, 6 = 32x8 with L2 prefetch of
- * the rows two planes ahead; -1 = automatic; staging applies to
+ * plane in place of the per-plane block barrier; -1 = automatic; staging applies to
  * shape 0 only), order (of the single pass's work items over the grid: 0 x
  * fastest, 1 the chunk fastest, 2 y fastest; -1 = automatic), grid (CTAs
  * launched; output only).  get reports what runs: the path, staging, tile and
