@@ -509,6 +509,16 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
         psi_plane(m0 + R);  // one plane ahead; the main loop computes m+R+1
         __syncthreads();
     }
+    // 2D: the thread's own populations of plane m+1 are loaded while plane m
+    // is computed (Q more registers), so their latency overlaps a whole plane
+    // instead of the short stage reduction before the force needs them
+    float fa[STAGED ? Q : 1];
+    if constexpr (STAGED) {
+        if (in_tile) {
+#pragma unroll
+            for (int q = 0; q < Q; q++) fa[q] = __ldg(pop + (own_cell + m0 * Lx + q * V));
+        }
+    }
     for (int m = m0; m < m1; m++) {
         int Z3[3];
 #pragma unroll
@@ -518,8 +528,17 @@ __device__ __forceinline__ void fused_tile(const float *__restrict__ pop, float 
         constexpr int NR = NoiseParams<L, float>::NR;
         SeedT st[NOISE ? NR : 1];
         if (in_tile && !OWN_TMA) {
+            if constexpr (STAGED) {
 #pragma unroll
-            for (int q = 0; q < Q; q++) f[q] = __ldg(pop + (g + q * V));
+                for (int q = 0; q < Q; q++) f[q] = fa[q];
+                if (m + 1 < m1) {
+#pragma unroll
+                    for (int q = 0; q < Q; q++) fa[q] = __ldg(pop + (own_cell + (m + 1) * Lx + q * V));
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < Q; q++) f[q] = __ldg(pop + (g + q * V));
+            }
             // generator states with the populations: their loads overlap the psi plane
             // (one generator per moment: the two-generator mode runs the two-pass kernel)
             if constexpr (NOISE) noise_load<L, SeedT, int>(0, seeds, (int64_t)V, (int64_t)g, st);

@@ -1893,9 +1893,8 @@ int64_t lattice_cells(const sclbm_batch *b, int i) {
 // Work items of the active lattices: tiles x runs of `chunk` marching planes.
 // A work item's planes are processed one after another (each a global-memory
 // round trip and a barrier), so the step time has a floor of about
-// (chunk + 2R) plane latencies; the chunk is the longest one that still gives
-// two items per resident CTA, and no shorter than BATCH_MIN_CHUNK (each item
-// re-reads 2R halo planes).
+// (chunk + 2R) plane latencies, while each item also re-reads 2R halo planes;
+// batch_plan weighs the two.
 void batch_items(const sclbm_batch *b, int chunk, std::vector<int4> &items) {
     items.clear();
     const int TX = b->ops->fused_tx, TY = b->ops->fused_ty;
@@ -1910,14 +1909,27 @@ void batch_items(const sclbm_batch *b, int chunk, std::vector<int4> &items) {
     }
 }
 
+// The plane run per item: the one (of 32, 16, .., BATCH_MIN_CHUNK) with the
+// fewest sequential plane passes per step, waves x (chunk + 2R), waves =
+// items / resident CTAs rounded up; on a tie the longer run (less halo
+// re-read).  Many cells: many waves, and the long run wins by its smaller
+// halo share; few cells: one wave, and the run shrinks until a second wave
+// would be needed.
 int batch_plan(sclbm_batch *b) {
     const int resident = b->sms * b->ops->fused_occupancy(0, 0, 0);
+    const int R = b->ops->fused_r;
     int chunk = BATCH_CHUNK;
-    std::vector<int4> items;
-    batch_items(b, chunk, items);
-    while (chunk > BATCH_MIN_CHUNK && (int)items.size() < 2 * resident) {
-        chunk = std::max(BATCH_MIN_CHUNK, chunk / 2);
-        batch_items(b, chunk, items);
+    int64_t best = -1;
+    std::vector<int4> items, trial;
+    for (int c = BATCH_CHUNK; c >= BATCH_MIN_CHUNK; c /= 2) {
+        batch_items(b, c, trial);
+        const int64_t waves = std::max<int64_t>(1, ((int64_t)trial.size() + resident - 1) / resident);
+        const int64_t passes = waves * (c + 2 * R);
+        if (best < 0 || passes < best) {
+            best = passes;
+            chunk = c;
+            items.swap(trial);
+        }
     }
     for (auto &g : b->graph)
         if (g) cudaGraphExecDestroy(g), g = nullptr;  // they hold the item count and grid
