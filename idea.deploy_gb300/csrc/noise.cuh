@@ -181,7 +181,8 @@ __device__ __forceinline__ T nonzero_state(T a) {
 
 // advance the states and form the random moments.  KIND (a CRNG_* value, or 0
 // for z.kind at run time): with the generator known at compile time only its
-// own update and conversion are emitted, not the three generators' selected
+// own update and conversion are emitted, instead of all three generators'
+// updates and a run-time selection among them
 template <class L, class Real, bool STRICT, class T, int KIND = 0>
 __device__ __forceinline__ void noise_compute(const NoiseParams<L, Real> &z, int indep, T *st, Real *rm) {
     constexpr int NR = NoiseParams<L, Real>::NR;
