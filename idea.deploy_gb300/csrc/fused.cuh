@@ -859,8 +859,15 @@ struct BatchInst {
 // Resident CTAs per SM as the single-lattice kernel's: four (BGK, paired
 // loads, 64 registers) or three (BGK, one halo cell per load, 80 registers),
 // no spills; two for the dense MRT operator.
-template <class L, class S, bool MRT, bool PAIRS = false>
-__global__ void __launch_bounds__(FusedShape<L, S>::NT, MRT ? 2 : (PAIRS ? 4 : 3))
+// TXB (2D only): tile width, 0 for the single-lattice kernel's 256 cells;
+// BATCH_TX_NARROW makes four times as many work items of a quarter the width
+// (the same cells and arithmetic, so bit-identical), with the same registers
+// per SM (twelve 64-thread CTAs for BGK)
+constexpr int BATCH_TX_NARROW = 64;
+constexpr int batch_min_blocks(bool mrt, bool pairs, int nt) { return (mrt ? 512 : (pairs ? 1024 : 768)) / nt; }
+template <class L, class S, bool MRT, bool PAIRS = false, int TXB = 0>
+__global__ void __launch_bounds__(FusedShape<L, S, TXB>::NT,
+                                  batch_min_blocks(MRT, PAIRS, FusedShape<L, S, TXB>::NT))
     k_fused_batch(const float *__restrict__ pop, float *__restrict__ pop_out,
                   const __grid_constant__ StepParams<L, S, float> p, const BatchInst *__restrict__ inst,
                   const int4 *__restrict__ items, const int n_items, const int Vtot, int *counter, const int parity) {
@@ -877,7 +884,8 @@ __global__ void __launch_bounds__(FusedShape<L, S>::NT, MRT ? 2 : (PAIRS ? 4 : 3
         const int4 w = items[it];  // lattice, x0, y0, m0 | m1 << 16
         const BatchInst I = inst[w.x];
         if (!I.active) continue;
-        fused_tile<L, S, MRT, void, false, PAIRS, 0, 0, 0, true>(pop + I.base, pop_out + I.base, Vtot, I.Lx, I.Ly,
+        static_assert(TXB == 0 || L::D == 2, "narrow batch tiles: 2D");
+        fused_tile<L, S, MRT, void, false, PAIRS, 0, TXB, 0, true>(pop + I.base, pop_out + I.base, Vtot, I.Lx, I.Ly,
                                                                  I.Lz, w.y, w.z,
                                                   w.w & 0xffff, w.w >> 16, I.neg_g, I.rho0, p, smem);
     }

@@ -62,8 +62,11 @@ struct KernelOps {
     int fused_stg_mask;  // STG_* variants built for this kernel set (0: none)
     int fused_tile_mask; // kTiles shapes built (bit t) for the paired single pass (bit 0: the default)
     // batches of lattices (FP32 only, else null)
+    // tx: tile width of a 2D batch (0: fused_tx; BATCH_TX_NARROW: the narrow tiles)
     cudaError_t (*batch_step)(const void *pop, void *pop_out, const void *sp, const BatchInst *inst, const int4 *items,
-                              int n_items, int Vtot, int *counter, int parity, int pairs, int grid, cudaStream_t st);
+                              int n_items, int Vtot, int *counter, int parity, int pairs, int tx, int grid,
+                              cudaStream_t st);
+    int (*batch_occupancy)(int pairs, int tx);  // resident CTAs per SM of the batch kernel
     cudaError_t (*batch_density)(const void *pop, void *dn, void *psi, const void *sp, const BatchInst *inst, int n_inst,
                                  int Vtot, int gx, cudaStream_t st);
     cudaError_t (*batch_moments)(const void *pop, const void *dn, const void *psi, void *u_old, const void *sp,
@@ -329,35 +332,67 @@ struct Ops {
         }
         return 0;
     }
+    template <bool PAIRS, int TXB>
+    static void batch_allow_smem() {
+        using SH = FusedShape<L, S, TXB>;
+        static bool done[64] = {};
+        int dev = 0;
+        cudaGetDevice(&dev);
+        if (dev < 0 || dev >= 64 || !done[dev]) {
+            cudaFuncSetAttribute(k_fused_batch<L, S, MRT, PAIRS, TXB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 SH::SMEM);
+            if (dev >= 0 && dev < 64) done[dev] = true;
+        }
+    }
+    template <bool PAIRS, int TXB>
+    static cudaError_t batch_launch(const void *pop, void *pop_out, const void *sp, const BatchInst *inst,
+                                    const int4 *items, int n_items, int Vtot, int *counter, int parity, int grid,
+                                    cudaStream_t st) {
+        using SH = FusedShape<L, S, TXB>;
+        batch_allow_smem<PAIRS, TXB>();
+        k_fused_batch<L, S, MRT, PAIRS, TXB><<<grid, SH::NT, SH::SMEM, st>>>(
+            (const float *)pop, (float *)pop_out, *static_cast<const SP *>(sp), inst, items, n_items, Vtot, counter,
+            parity);
+        return cudaGetLastError();
+    }
     static cudaError_t batch_step(const void *pop, void *pop_out, const void *sp, const BatchInst *inst,
                                   const int4 *items, int n_items, int Vtot, int *counter, int parity, int pairs,
-                                  int grid, cudaStream_t st) {
+                                  int tx, int grid, cudaStream_t st) {
         if constexpr (std::is_same<Real, float>::value) {
-            using SH = FusedShape<L, S>;
-            static bool done[64] = {};
-            int dev = 0;
-            cudaGetDevice(&dev);
-            if (dev < 0 || dev >= 64 || !done[dev]) {
-                cudaFuncSetAttribute(k_fused_batch<L, S, MRT>, cudaFuncAttributeMaxDynamicSharedMemorySize, SH::SMEM);
-                if constexpr (L::D == 3 && S::R % 2 == 0)
-                    cudaFuncSetAttribute(k_fused_batch<L, S, MRT, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         SH::SMEM);
-                if (dev >= 0 && dev < 64) done[dev] = true;
-            }
             if constexpr (L::D == 3 && S::R % 2 == 0) {
-                if (pairs) {
-                    k_fused_batch<L, S, MRT, true><<<grid, SH::NT, SH::SMEM, st>>>(
-                        (const float *)pop, (float *)pop_out, *static_cast<const SP *>(sp), inst, items, n_items, Vtot,
-                        counter, parity);
-                    return cudaGetLastError();
-                }
+                if (pairs)
+                    return batch_launch<true, 0>(pop, pop_out, sp, inst, items, n_items, Vtot, counter, parity, grid,
+                                                 st);
             }
-            k_fused_batch<L, S, MRT><<<grid, SH::NT, SH::SMEM, st>>>((const float *)pop, (float *)pop_out,
-                                                                     *static_cast<const SP *>(sp), inst, items,
-                                                                     n_items, Vtot, counter, parity);
-            return cudaGetLastError();
+            if constexpr (L::D == 2) {
+                if (tx == BATCH_TX_NARROW)
+                    return batch_launch<false, BATCH_TX_NARROW>(pop, pop_out, sp, inst, items, n_items, Vtot, counter,
+                                                                parity, grid, st);
+            }
+            if (tx != 0 && tx != FusedShape<L, S>::TX) return cudaErrorInvalidValue;
+            return batch_launch<false, 0>(pop, pop_out, sp, inst, items, n_items, Vtot, counter, parity, grid, st);
         }
         return cudaErrorNotSupported;
+    }
+    template <bool PAIRS, int TXB>
+    static int batch_occ() {
+        using SH = FusedShape<L, S, TXB>;
+        int b = 0;
+        batch_allow_smem<PAIRS, TXB>();
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_fused_batch<L, S, MRT, PAIRS, TXB>, SH::NT, SH::SMEM);
+        return b > 0 ? b : 1;
+    }
+    static int batch_occupancy(int pairs, int tx) {
+        if constexpr (std::is_same<Real, float>::value) {
+            if constexpr (L::D == 3 && S::R % 2 == 0) {
+                if (pairs) return batch_occ<true, 0>();
+            }
+            if constexpr (L::D == 2) {
+                if (tx == BATCH_TX_NARROW) return batch_occ<false, BATCH_TX_NARROW>();
+            }
+            return batch_occ<false, 0>();
+        }
+        return 1;
     }
     static cudaError_t batch_density(const void *pop, void *dn, void *psi, const void *sp, const BatchInst *inst,
                                      int n_inst, int Vtot, int gx, cudaStream_t st) {
@@ -591,7 +626,7 @@ struct Ops {
                                     &fcs, &velocity, &density_walls, &fcs_walls, &init_pop, &grids,
                                     f32 ? &fused : nullptr, SH::TX, SH::TY, SH::R,
                                     f32 ? &fused_occupancy : nullptr, STG_MASK, TILE_MASK,
-                                    f32 ? &batch_step : nullptr, f32 ? &batch_density : nullptr,
+                                    f32 ? &batch_step : nullptr, &batch_occupancy, f32 ? &batch_density : nullptr,
                                     f32 ? &batch_moments : nullptr, f32 ? &batch_mass : nullptr,
                                     f32 ? &batch_add_rest : nullptr, f32 ? &batch_probe : nullptr,
                                     sizeof(NP), MRT ? nullptr : &fill_noise, MRT ? nullptr : &fcs_noise,

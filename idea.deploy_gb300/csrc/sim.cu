@@ -1835,6 +1835,7 @@ struct sclbm_batch {
     int64_t Vtot = 0;
     std::vector<int4> items;
     int4 *items_d = nullptr;
+    size_t items_cap = 0;  // work items items_d holds
     int *counter = nullptr;  // [2] work queues, one per step parity
     float *wq_d = nullptr;
     const KernelOps *ops = nullptr;
@@ -1848,6 +1849,7 @@ struct sclbm_batch {
     float *delta_d = nullptr;   // [n] rest-population corrections
     int gx = 1, grid = 1, chunk = 32;
     int pairs = 0;          // 3D, even radius, every Lx and first cell even: paired halo loads
+    int tx = 0;             // 2D tile width (0: the single-lattice kernel's; BATCH_TX_NARROW)
     std::vector<int> home;  // buffer holding a retired lattice's state (-1 while active)
     std::vector<int64_t> steps;
     bool pop_set = false;
@@ -1897,7 +1899,7 @@ int64_t lattice_cells(const sclbm_batch *b, int i) {
 // batch_plan weighs the two.
 void batch_items(const sclbm_batch *b, int chunk, std::vector<int4> &items) {
     items.clear();
-    const int TX = b->ops->fused_tx, TY = b->ops->fused_ty;
+    const int TX = b->tx ? b->tx : b->ops->fused_tx, TY = b->ops->fused_ty;
     for (int i = 0; i < b->n; i++) {
         if (!b->inst[i].active) continue;
         const BatchInst &I = b->inst[i];
@@ -1916,7 +1918,7 @@ void batch_items(const sclbm_batch *b, int chunk, std::vector<int4> &items) {
 // halo share; few cells: one wave, and the run shrinks until a second wave
 // would be needed.
 int batch_plan(sclbm_batch *b) {
-    const int resident = b->sms * b->ops->fused_occupancy(0, 0, 0);
+    const int resident = b->sms * b->ops->batch_occupancy(b->pairs, b->tx);
     const int R = b->ops->fused_r;
     int chunk = BATCH_CHUNK;
     int64_t best = -1;
@@ -1931,6 +1933,8 @@ int batch_plan(sclbm_batch *b) {
             items.swap(trial);
         }
     }
+    if (items.size() > b->items_cap)
+        return fail(SCLBM_ERR_STATE, "%zu work items, room for %zu", items.size(), b->items_cap);
     for (auto &g : b->graph)
         if (g) cudaGraphExecDestroy(g), g = nullptr;  // they hold the item count and grid
     b->items.swap(items);
@@ -1945,7 +1949,7 @@ int batch_plan(sclbm_batch *b) {
 
 int batch_launch_step(sclbm_batch *b) {
     cudaError_t e = b->ops->batch_step(b->pop[b->cur], b->pop[b->cur ^ 1], b->sp.data(), b->inst_d, b->items_d,
-                                       (int)b->items.size(), (int)b->Vtot, b->counter, b->cur, b->pairs, b->grid,
+                                       (int)b->items.size(), (int)b->Vtot, b->counter, b->cur, b->pairs, b->tx, b->grid,
                                        b->st);
     if (e != cudaSuccess) return fail(SCLBM_ERR_CUDA, "batch step: %s", cudaGetErrorString(e));
     b->cur ^= 1;
@@ -2100,8 +2104,12 @@ int sclbm_batch_create(const sclbm_params *p, int n, const int *sizes, const dou
     if (!rc) rc = balloc(b, (void **)&b->partials, (size_t)n * b->gx * BATCH_NV * sizeof(double));
     if (!rc) rc = balloc(b, (void **)&b->inst_d, sizeof(BatchInst) * n);
     {
-        std::vector<int4> most;  // the longest item list: every lattice, the shortest chunk
+        // the longest item list: every lattice, the shortest chunk, the narrowest tiles
+        std::vector<int4> most;
+        b->tx = b->D == 2 ? BATCH_TX_NARROW : 0;
         batch_items(b, BATCH_MIN_CHUNK, most);
+        b->tx = 0;
+        b->items_cap = most.size();
         if (!rc) rc = balloc(b, (void **)&b->items_d, sizeof(int4) * most.size());
     }
     if (!rc) rc = balloc(b, (void **)&b->counter, 2 * sizeof(int));
@@ -2320,6 +2328,16 @@ int sclbm_batch_restore_mass(sclbm_batch *b, const double *target, double *befor
     if (e != cudaSuccess) return fail(SCLBM_ERR_CUDA, "batch mass correction: %s", cudaGetErrorString(e));
     CUDA_TRY(cudaStreamSynchronize(b->st));
     return SCLBM_OK;
+}
+
+int sclbm_batch_set_tile_width(sclbm_batch *b, int tx) {
+    if (!b) return fail(SCLBM_ERR_ARG, "null handle");
+    if (tx != 0 && !(b->D == 2 && tx == BATCH_TX_NARROW))
+        return fail(SCLBM_ERR_ARG, "tile width %d (0, or %d for 2D batches)", tx, BATCH_TX_NARROW);
+    if (tx == b->tx) return SCLBM_OK;
+    DevGuard dg(b->device);
+    b->tx = tx;
+    return batch_plan(b);
 }
 
 int sclbm_batch_set_probe_radius(sclbm_batch *b, int rad) {

@@ -107,6 +107,7 @@ SIGNATURES = {
     'sclbm_batch_init_lattice': [_P, ctypes.c_int],
     'sclbm_batch_probe': [_P, _P, _P],
     'sclbm_batch_set_probe_radius': [_P, ctypes.c_int],
+    'sclbm_batch_set_tile_width': [_P, ctypes.c_int],
     'sclbm_restore_mass': [_P, _D, _DP],
     'sclbm_set_walls': [_P, _P, _P],
     'sclbm_noise_counts': [ctypes.c_int, ctypes.c_int, ctypes.c_int, _IP, _IP],

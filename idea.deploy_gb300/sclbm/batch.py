@@ -112,6 +112,10 @@ class Batch:
         _lib.call('sclbm_batch_restore_mass', self.h, _lib.ptr(t), _lib.ptr(before))
         return before
 
+    def set_tile_width(self, tx):
+        """2D batches: 0 (256-cell tiles, the default) or 64; bit-identical results."""
+        _lib.call('sclbm_batch_set_tile_width', self.h, int(tx))
+
     def set_probe_radius(self, rad):
         """probe() returns means over the cube of side 2 rad + 1 about each cell."""
         _lib.call('sclbm_batch_set_probe_radius', self.h, int(rad))

@@ -140,6 +140,11 @@ def ragged_sweep(radii, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, che
     # populations then keep most of their FP32 digits
     b = Batch_(XIStencils['D2Q9' if dim == 2 else 'D3Q19'], FStencils[stencil], sizes, G, list(rho_g), tau=tau,
                device=device)
+    if dim == 2:
+        # 64-cell tiles: boxes of 32 .. 288 cells leave 256-cell rows part
+        # empty, and a few boxes make too few items to fill the GPU (same
+        # results, bit for bit; ~30 % shorter steps with 20-30 boxes active)
+        b.set_tile_width(64)
     for i in range(n):
         b.set_density(i, init[i] if init is not None else cold(i))
     b.init_populations()

@@ -388,6 +388,12 @@ SCLBM_API int sclbm_batch_probe(sclbm_batch *b, double *n_in, double *n_out);
  * biases the mean by ~1e-5 of the Laplace pressure, so the sweeps keep single
  * cells.  No counterpart in the reference. */
 SCLBM_API int sclbm_batch_set_probe_radius(sclbm_batch *b, int rad);
+/* tile width of a 2D batch's work items: 0 (the default, the single-lattice
+ * kernel's 256 cells) or 64 (four times as many items of a quarter the width,
+ * for batches whose lattices are too few or too small to fill the GPU with
+ * 256-cell rows).  The results are bit-identical.  3D batches take 0 only.
+ * No counterpart in the reference. */
+SCLBM_API int sclbm_batch_set_tile_width(sclbm_batch *b, int tx);
 
 /* ---------------------------------------------------------------------------
  * Warm-start surrogate: an MLP 5 -> 64 -> 64 -> 64 -> 1 with SiLU, BF16

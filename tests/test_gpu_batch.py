@@ -87,6 +87,40 @@ def test_batch_retires_lattices_individually():
     b.close()
 
 
+@pytest.mark.parametrize('st', ['D2E4', 'D2E8'])
+def test_narrow_2d_tiles_bit_identical(st):
+    """64-cell tiles (four times the work items) step every lattice bit for
+    bit as the default 256-cell tiles, also across retirement and re-planning;
+    lattices narrower than, equal to and wider than either tile."""
+    dims = [(32, 32), (50, 40), (64, 70), (100, 100), (224, 96), (300, 36)]
+    G, rho0 = [-4.5, -4.8, -4.6, -4.6, -4.7, -4.5], [0.2, 1.0, 2.0, 0.5, 0.22, 0.3]
+    n0 = densities(dims)
+    out = []
+    for tx in (0, 64):
+        b = Batch(XIStencils['D2Q9'], FStencils[st], dims, G, rho0)
+        b.set_tile_width(tx)
+        for i, n in enumerate(n0):
+            b.set_density(i, n)
+        b.init_populations()
+        b.step(45)
+        b.set_active([1, 0, 1, 1, 0, 1])
+        b.step(38)
+        out.append([b.get_density(i) for i in range(len(dims))])
+        b.close()
+    for i in range(len(dims)):
+        assert np.isfinite(out[0][i]).all(), i
+        assert np.array_equal(out[0][i], out[1][i]), i
+
+
+def test_narrow_tiles_refused_in_3d():
+    lat, st, dims, G, rho0 = CASES['3d']
+    b = Batch(XIStencils[lat], FStencils[st], dims, G, rho0)
+    with pytest.raises(_lib.SclbmError):
+        b.set_tile_width(64)
+    b.set_tile_width(0)
+    b.close()
+
+
 def test_batch_rejects_bad_input():
     lat, st = 'D2Q9', 'D2E8'
     with pytest.raises(_lib.SclbmError):
