@@ -144,13 +144,15 @@ __device__ __forceinline__ void tma_load_4d(void *dst, const CUtensorMap *map, u
 // buffer as it is (no thread leaves the block's barriers); later waits of the
 // launch then return at once.
 constexpr int MBAR_POLLS = 1 << 20;
-__device__ __forceinline__ void mbar_wait_bounded(uint64_t *bar, unsigned parity, int *err, bool &dead) {
+__device__ __forceinline__ void mbar_wait_bounded(uint64_t *bar, unsigned parity, int *err, bool &dead,
+                                                  int polls = MBAR_POLLS) {
     if (dead) return;
-    for (int i = 0; i < MBAR_POLLS; i++)
+    for (int i = 0; i < polls; i++)
         if (mbar_try_wait(bar, parity)) return;
     dead = true;
     if (err) atomicOr(err, 1);
 }
+
 
 __device__ __forceinline__ void cp_async4(float *smem, const float *gmem) {
     const unsigned s = (unsigned)__cvta_generic_to_shared(smem);

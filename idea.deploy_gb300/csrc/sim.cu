@@ -116,6 +116,25 @@ __global__ void __launch_bounds__(RED_THREADS) k_reduce_pop(const Real *__restri
 }
 
 // add delta to the rest population (q = 0) of every cell
+// Self-test of the bounded wait: an mbarrier that expects two arrivals gets
+// one, so its phase never completes; the wait gives up after `polls` polls,
+// records it in *err as the single-pass variants do, and the kernel returns.
+// *err bit 1: the phase completed, which must not happen.
+__global__ void k_bounded_wait_selftest(int *err, int polls) {
+    __shared__ uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 2);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        mbar_arrive(&bar);
+        bool dead = false;
+        mbar_wait_bounded(&bar, 0, err, dead, polls);
+        if (!dead) atomicOr(err, 2);
+    }
+}
+
 template <class Real>
 __global__ void __launch_bounds__(RED_THREADS) k_add_rest(Real *__restrict__ pop0, int64_t V, Real delta) {
     for (int64_t g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; g < V; g += (int64_t)gridDim.x * blockDim.x)
@@ -1199,9 +1218,45 @@ int sclbm_step(sclbm_sim *s, int64_t nsteps) {
 int check_flag(sclbm_sim *s) {
     if (s->flag_host && *(volatile int *)s->flag_host) {
         *s->flag_host = 0;
-        return fail(SCLBM_ERR_CUDA, "a staged single-pass kernel gave up waiting for its TMA loads "
-                                    "(results of the last steps are invalid)");
+        return fail(SCLBM_ERR_CUDA, "a single-pass kernel gave up waiting on an mbarrier (TMA staging or the "
+                                    "mbarrier psi ring); results of the last steps are invalid");
     }
+    return SCLBM_OK;
+}
+
+int sclbm_selftest_bounded_wait(int device, int polls, int *gave_up, double *ms) {
+    clear_error();
+    if (!gave_up || polls < 1 || polls > MBAR_POLLS)
+        return fail(SCLBM_ERR_ARG, "polls %d (1 .. %d), gave_up required", polls, MBAR_POLLS);
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n) {
+        cudaGetLastError();
+        return fail(SCLBM_ERR_NODEVICE, "device %d", device);
+    }
+    DevGuard dg(device);
+    int *err = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaMalloc((void **)&err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(err, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    if (e == cudaSuccess) e = cudaEventRecord(e0);
+    if (e == cudaSuccess) {
+        k_bounded_wait_selftest<<<1, 32>>>(err, polls);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaEventRecord(e1);
+    if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+    int flag = 0;
+    if (e == cudaSuccess) e = cudaMemcpy(&flag, err, sizeof(int), cudaMemcpyDeviceToHost);
+    float t = 0.f;
+    if (e == cudaSuccess && ms) e = cudaEventElapsedTime(&t, e0, e1);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (err) cudaFree(err);
+    if (e != cudaSuccess) return fail(SCLBM_ERR_CUDA, "bounded-wait self-test: %s", cudaGetErrorString(e));
+    *gave_up = flag;
+    if (ms) *ms = t;
     return SCLBM_OK;
 }
 

@@ -108,6 +108,8 @@ SIGNATURES = {
     'sclbm_batch_probe': [_P, _P, _P],
     'sclbm_batch_set_probe_radius': [_P, ctypes.c_int],
     'sclbm_batch_set_tile_width': [_P, ctypes.c_int],
+    'sclbm_selftest_bounded_wait': [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
+                                    ctypes.POINTER(ctypes.c_double)],
     'sclbm_restore_mass': [_P, _D, _DP],
     'sclbm_set_walls': [_P, _P, _P],
     'sclbm_noise_counts': [ctypes.c_int, ctypes.c_int, ctypes.c_int, _IP, _IP],
@@ -171,6 +173,15 @@ def call(name, *args):
 
 def ptr(a):
     return ctypes.c_void_p(a.ctypes.data)
+
+
+def selftest_bounded_wait(device=0, polls=1 << 16):
+    """One block waits on an mbarrier that cannot complete and gives up after
+    ``polls`` polls (the limit of the single-pass variants' waits is 2^20);
+    returns (gave_up flag, milliseconds)."""
+    flag, ms = ctypes.c_int(), ctypes.c_double()
+    call('sclbm_selftest_bounded_wait', int(device), int(polls), ctypes.byref(flag), ctypes.byref(ms))
+    return flag.value, ms.value
 
 
 def dptr(a):

@@ -239,6 +239,15 @@ SCLBM_API int sclbm_set_transfer(sclbm_sim *s, int mode, int *pageable_access);
  * waiting); sclbm_sync waits for everything enqueued on the handle */
 SCLBM_API int sclbm_step(sclbm_sim *s, int64_t nsteps);
 SCLBM_API int sclbm_sync(sclbm_sim *s);
+
+/* self-test of the bounded device waits (the mbarrier waits of the staged and
+ * mbarrier-ring single-pass variants): one block waits on an mbarrier whose
+ * phase cannot complete (two arrivals expected, one made), gives up after
+ * `polls` polls (1 .. 2^20, the variants' limit) and returns.  *gave_up: 1
+ * when the wait gave up as it must (bit 2: the phase completed, an error);
+ * *ms (optional): the launch's duration.  The device stays usable: nothing
+ * faults or hangs.  No counterpart in the reference. */
+SCLBM_API int sclbm_selftest_bounded_wait(int device, int polls, int *gave_up, double *ms);
 /* as sclbm_step, bracketed by CUDA events on the handle's stream; waits and
  * returns the elapsed device time in milliseconds */
 SCLBM_API int sclbm_step_timed(sclbm_sim *s, int64_t nsteps, double *ms);
