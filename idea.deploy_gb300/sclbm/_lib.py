@@ -177,7 +177,7 @@ def ptr(a):
 
 def selftest_bounded_wait(device=0, polls=1 << 16):
     """One block waits on an mbarrier that cannot complete and gives up after
-    ``polls`` polls (the limit of the single-pass variants' waits is 2^20);
+    ``polls`` polls (the limit of the single-pass variants' waits is 2^18);
     returns (gave_up flag, milliseconds)."""
     flag, ms = ctypes.c_int(), ctypes.c_double()
     call('sclbm_selftest_bounded_wait', int(device), int(polls), ctypes.byref(flag), ctypes.byref(ms))

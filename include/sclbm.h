@@ -243,7 +243,7 @@ SCLBM_API int sclbm_sync(sclbm_sim *s);
 /* self-test of the bounded device waits (the mbarrier waits of the staged and
  * mbarrier-ring single-pass variants): one block waits on an mbarrier whose
  * phase cannot complete (two arrivals expected, one made), gives up after
- * `polls` polls (1 .. 2^20, the variants' limit) and returns.  *gave_up: 1
+ * `polls` polls (1 .. 2^18, the variants' limit: ~1 s) and returns.  *gave_up: 1
  * when the wait gave up as it must (bit 2: the phase completed, an error);
  * *ms (optional): the launch's duration.  The device stays usable: nothing
  * faults or hangs.  No counterpart in the reference. */
