@@ -877,6 +877,9 @@ __global__ void __launch_bounds__(FusedShape<L, S, TXB>::NT,
                   const int4 *__restrict__ items, const int n_items, const int Vtot, int *counter, const int parity) {
     extern __shared__ float smem[];
     __shared__ int next;
+    // launched as a programmatic dependent of the previous step: nothing is
+    // read or written before that step has completed
+    asm volatile("griddepcontrol.wait;\n" ::: "memory");
     // the other parity's queue is reset for the next step (not used by this one)
     if (blockIdx.x == 0 && threadIdx.x == 0) counter[parity ^ 1] = 0;
     while (true) {
@@ -884,7 +887,11 @@ __global__ void __launch_bounds__(FusedShape<L, S, TXB>::NT,
         __syncthreads();
         const int it = next;
         __syncthreads();
-        if (it >= n_items) break;
+        if (it >= n_items) {
+            // no work left for this CTA: the next step may start placing its CTAs
+            asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory");
+            break;
+        }
         const int4 w = items[it];  // lattice, x0, y0, m0 | m1 << 16
         const BatchInst I = inst[w.x];
         if (!I.active) continue;

@@ -350,10 +350,21 @@ struct Ops {
                                     cudaStream_t st) {
         using SH = FusedShape<L, S, TXB>;
         batch_allow_smem<PAIRS, TXB>();
-        k_fused_batch<L, S, MRT, PAIRS, TXB><<<grid, SH::NT, SH::SMEM, st>>>(
-            (const float *)pop, (float *)pop_out, *static_cast<const SP *>(sp), inst, items, n_items, Vtot, counter,
-            parity);
-        return cudaGetLastError();
+        // programmatic dependent launch: a step's CTAs are placed while the
+        // previous step's last items finish, and wait (griddepcontrol.wait)
+        // for its completion before they read anything
+        cudaLaunchConfig_t cfg = {};
+        cfg.gridDim = dim3(grid);
+        cfg.blockDim = dim3(SH::NT);
+        cfg.dynamicSmemBytes = SH::SMEM;
+        cfg.stream = st;
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[0].val.programmaticStreamSerializationAllowed = 1;
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        return cudaLaunchKernelEx(&cfg, k_fused_batch<L, S, MRT, PAIRS, TXB>, (const float *)pop, (float *)pop_out,
+                                  *static_cast<const SP *>(sp), inst, items, n_items, Vtot, counter, parity);
     }
     static cudaError_t batch_step(const void *pop, void *pop_out, const void *sp, const BatchInst *inst,
                                   const int4 *items, int n_items, int Vtot, int *counter, int parity, int pairs,
