@@ -246,7 +246,7 @@ def make_sim(precision, device, literals='exact', box=None, g=None, rho0=None):
                     collision=_lib.COLL_MRT, mrt_s=S,
                     precision=_lib.FP32_SHIFTED if precision == 'fp32' else _lib.FP64,
                     rho0=0.5 * (RHO_L + RHO_G) if rho0 is None else rho0, device=device,
-                    literals=_lib.LIT_EXACT if literals == 'exact' else _lib.LIT_ROUND15)
+                    literals={'exact': _lib.LIT_EXACT, 'factored': _lib.LIT_FACTORED}.get(literals, _lib.LIT_ROUND15))
 
 
 def stable_twin(dev, steps, ms_headline):
@@ -332,12 +332,17 @@ def sweep_leg(dev, max_steps=100000, coex_steps=100000):
     default run: the batched FP32 path and the plain FP64 path droplet by
     droplet, both stopped by the same criterion (the Laplace pressure calm to
     2e-5 over 4 checks of 500 steps); wall time to converge, speed-up, and the
-    Laplace-pressure error of the batch against the FP64 runs."""
-    from sclbm import sweep
+    Laplace-pressure error of the batch against the FP64 runs.  The plain arm
+    runs the fastest FP64 arithmetic (the BGK operator factored, exact
+    coefficients, FMA); the same arm with the reference's expanded operator is
+    timed beside it."""
+    from sclbm import sweep, _lib
     r = sweep.run_sweep(n=64, max_steps=max_steps, coex_steps=coex_steps, plain=True, device=dev,
-                        plain_stop_at_dp=True)
+                        plain_stop_at_dp=True, plain_literals=_lib.LIT_FACTORED,
+                        plain_extra_literals=(_lib.LIT_EXACT,))
     b = r['batch']
     plain = r['plain']
+    expanded = r['plain_extra'][_lib.LIT_EXACT]
     both = [j for j, p in enumerate(plain)
             if p is not None and p['status'] == 'converged' and b['status'][j] == 'converged']
     errs = np.array([abs(b['dp'][j] - plain[j]['dp']) / abs(plain[j]['dp']) for j in both])
@@ -347,9 +352,13 @@ def sweep_leg(dev, max_steps=100000, coex_steps=100000):
                            'status': {str(k): int((b['status'] == k).sum()) for k in set(b['status'])},
                            'steps_max': int(np.max(b['steps']))},
             'plain_fp64': {'wall_s': round(r['plain_wall_s'], 3),
+                           'arithmetic': 'FP64, BGK operator factored by opposite directions, exact coefficients, FMA',
                            'status': {k: sum(1 for p in plain if p is not None and p['status'] == k)
                                       for k in ('converged', 'max_steps', 'diverged')}},
             'speedup_wall': round(r['plain_wall_s'] / b['wall_s'], 2),
+            'plain_fp64_expanded': {'wall_s': round(expanded['wall_s'], 3),
+                                    'arithmetic': "FP64, the reference's expanded operator, exact coefficients, FMA",
+                                    'speedup_wall': round(expanded['wall_s'] / b['wall_s'], 2)},
             'dp_rel_err_vs_fp64': {'median': float(np.median(errs)) if errs.size else None,
                                    'max': float(errs.max()) if errs.size else None,
                                    'within_1e-5': int((errs <= 1e-5).sum()), 'n': int(errs.size)},
@@ -512,7 +521,8 @@ def run_ours(a, dist):
         # exact coefficients, and the reference's arithmetic (its literals and
         # evaluation order, no FMA; GB300's FP64 rate bounds both)
         out['fp64'] = {}
-        for lit, key in (('exact', 'fused_arithmetic'), ('round15', 'reference_arithmetic')):
+        for lit, key in (('factored', 'factored_arithmetic'), ('exact', 'fused_arithmetic'),
+                         ('round15', 'reference_arithmetic')):
             s64 = make_sim('fp64', dev, literals=lit)
             s64.set_density(n0)
             s64.set_velocity(np.zeros(3 * V))
@@ -756,11 +766,15 @@ def run_sweep3d_mode(a):
     """3D batched droplets (256 D3Q19 E6 droplets in 96^3 boxes, FP32 batches)
     against the plain FP64 path on a timed sample, extrapolated."""
     from sclbm import sweep
-    r = sweep.run_sweep3d(n=a.sweep3d_n, max_steps=a.sweep3d_max_steps, plain_sample=a.sweep3d_plain)
+    from sclbm import _lib
+    r = sweep.run_sweep3d(n=a.sweep3d_n, max_steps=a.sweep3d_max_steps, plain_sample=a.sweep3d_plain,
+                          plain_literals=_lib.LIT_FACTORED if a.sweep3d_plain_factored else None)
     b = r['batch']
     ok = b['status'] == 'converged'
     out = {'metric': 'D3Q19 E6 batched droplets (96^3 boxes): time to converge, batched FP32 vs plain FP64',
            'unit': 's', 'config': r['config'],
+           'plain_arithmetic': ('FP64, BGK operator factored, exact coefficients, FMA' if a.sweep3d_plain_factored
+                                else "FP64, the reference's expanded operator, exact coefficients, FMA"),
            'batch': {'wall_s': round(b['wall_s'], 2), 'batches': b['batches'],
                      'status': {str(k): int((b['status'] == k).sum()) for k in set(b['status'])},
                      'steps_mean_converged': float(b['steps'][ok].mean()) if ok.any() else None,
@@ -797,6 +811,8 @@ def main():
     ap.add_argument('--sweep3d-n', type=int, default=256)
     ap.add_argument('--sweep3d-max-steps', type=int, default=20000)
     ap.add_argument('--sweep3d-plain', type=int, default=8)
+    ap.add_argument('--sweep3d-plain-expanded', dest='sweep3d_plain_factored', action='store_false',
+                    help="plain FP64 sample with the reference's expanded operator instead of the factored one")
     ap.add_argument('--warmstart3d', action='store_true', help='learned warm start of the 3D batched droplets')
     ap.add_argument('--ws3d-profiles', type=int, default=128)
     ap.add_argument('--ws-profiles', type=int, default=4096)

@@ -33,6 +33,7 @@ struct StepParams {
     Real neg_g;     // -G
     int psi_kind;
     int a_nonzero;  // BGK: 1 - omega != 0
+    int factored;   // FP64 BGK (SCLBM_LIT_FACTORED): the collision factored by opposite directions
     Real sw[QE][D]; // signed force weights e_{a,d} * w_a
     Real A[Q][Q];   // population operator (BGK: diagonal used)
     Real B[Q][K];   // monomial coefficients
@@ -330,6 +331,73 @@ __device__ __forceinline__ void collide_cell(const Real *f, Real d, Real n, cons
     }
 }
 
+// index of the lattice velocity opposite to xi_q (a table built once per lattice)
+template <class L>
+struct OppositeQ {
+    int v[L::Q];
+    constexpr OppositeQ() : v() {
+        for (int q = 0; q < L::Q; q++) {
+            v[q] = q;
+            for (int k = 0; k < L::Q; k++) {
+                bool same = true;
+                for (int d = 0; d < L::D; d++) same = same && (L::xi(k, d) == -L::xi(q, d));
+                if (same) {
+                    v[q] = k;
+                    break;
+                }
+            }
+        }
+    }
+};
+template <class L>
+SCLBM_HD constexpr int opposite_q(int q) {
+    constexpr OppositeQ<L> t{};
+    return t.v[q];
+}
+
+// BGK + Guo in FP64 with the operator factored by opposite directions (the
+// single FP32 pass uses the same form): with c2 = 1/3, eu = xi_q.u, eF = xi_q.F,
+//   f*_q = (1-w) f_q + w_q [C0 + eu (a eu + b + c eF) + d eF],
+//   C0 = w n - 1.5 w n u^2 - 3 (1-w/2) u.F, a = 4.5 w n, b = 3 w n,
+//   c = 9 (1-w/2), d = 3 (1-w/2)
+// (the 2nd-order Hermite equilibrium plus the Guo term, Collisions.py:163-185,
+// Forcings.py:104-127); a direction and its opposite share the even part
+// C0 + a eu^2 + c eu eF and take the odd part b eu + d eF with opposite signs.
+// FP64 storage has no shift (rho0 = 0), so d = n.  Exact coefficients, FMA:
+// equal to the expanded form up to rounding.
+template <class L, class S>
+__device__ __forceinline__ void bgk_factored(const double *f, double d, double n, const double *u,
+                                             const double *F, const StepParams<L, S, double> &p, double *out) {
+    constexpr int D = L::D, Q = L::Q;
+    double u2 = 0.0, uF = 0.0;
+#pragma unroll
+    for (int c = 0; c < D; c++) {
+        u2 = fma(u[c], u[c], u2);
+        uF = fma(u[c], F[c], uF);
+    }
+    const double C0 = p.omega * d - p.om15 * n * u2 - p.fd * uF;
+    const double a = p.om45 * n, b = p.om3 * n;
+#pragma unroll
+    for (int q = 0; q < Q; q++) {
+        const int qb = opposite_q<L>(q);
+        if (qb < q) continue;
+        double eu = 0.0, eF = 0.0;
+#pragma unroll
+        for (int c = 0; c < D; c++) {
+            if (L::xi(q, c) > 0) { eu += u[c]; eF += F[c]; }
+            if (L::xi(q, c) < 0) { eu -= u[c]; eF -= F[c]; }
+        }
+        const double even = C0 + eu * fma(a, eu, p.fc * eF);
+        const double odd = fma(b, eu, p.fd * eF);
+        const double rq = p.wq[q] * (even + odd);
+        out[q] = p.a_nonzero ? fma(p.A[q][q], f[q], rq) : rq;
+        if (qb != q) {
+            const double rqb = p.wq[qb] * (even - odd);
+            out[qb] = p.a_nonzero ? fma(p.A[qb][qb], f[qb], rqb) : rqb;
+        }
+    }
+}
+
 template <class L, class S, class Real, bool STRICT>
 __device__ __forceinline__ void force_velocity(const Real *__restrict__ psi, const Cell<L::D> &c, int64_t g,
                                                const StepParams<L, S, Real> &p, const Real *f, Real n, Real *F,
@@ -360,8 +428,17 @@ __global__ void __launch_bounds__(128) k_fcs(const Real *__restrict__ pop, Real 
         Real F[D], u[D];
         force_velocity<L, S, Real, STRICT>(psi, c, g, p, f, n, F, u);
         Real out[Q];
+        bool done = false;
+        if constexpr (!MRT && !STRICT && std::is_same<Real, double>::value) {
+            if (p.factored) {
+                bgk_factored<L, S>(f, d, n, u, F, p, out);
+                done = true;
+            }
+        }
+        if (!done) {
 #pragma unroll
-        for (int q = 0; q < Q; q++) collide_cell<L, S, MRT, Real, STRICT>(f, d, n, u, F, q, p, out[q]);
+            for (int q = 0; q < Q; q++) collide_cell<L, S, MRT, Real, STRICT>(f, d, n, u, F, q, p, out[q]);
+        }
         if constexpr (std::is_same<Real, float>::value) {
             // FP32 storage: rest population from mass conservation (as the single-pass kernel)
             Real rest = d;
@@ -387,28 +464,6 @@ __global__ void __launch_bounds__(128) k_fcs(const Real *__restrict__ pop, Real 
 // populations unchanged from buffer to buffer (the reference leaves them
 // stale), so the total mass stays constant.
 // ---------------------------------------------------------------------------
-template <class L>
-struct OppositeQ {
-    int v[L::Q];
-    constexpr OppositeQ() : v() {
-        for (int q = 0; q < L::Q; q++) {
-            v[q] = q;
-            for (int k = 0; k < L::Q; k++) {
-                bool same = true;
-                for (int d = 0; d < L::D; d++) same = same && (L::xi(k, d) == -L::xi(q, d));
-                if (same) {
-                    v[q] = k;
-                    break;
-                }
-            }
-        }
-    }
-};
-template <class L>
-SCLBM_HD constexpr int opposite_q(int q) {
-    constexpr OppositeQ<L> t{};
-    return t.v[q];
-}
 
 template <class L, class Real>
 __global__ void __launch_bounds__(256) k_density_psi_walls(const Real *__restrict__ pop, Real *__restrict__ dn,
@@ -453,8 +508,17 @@ __global__ void __launch_bounds__(128) k_fcs_walls(const Real *__restrict__ pop,
         Real F[D], u[D];
         force_velocity<L, S, Real, STRICT>(psi, c, g, p, f, n, F, u);
         Real out[Q];
+        bool done = false;
+        if constexpr (!MRT && !STRICT && std::is_same<Real, double>::value) {
+            if (p.factored) {
+                bgk_factored<L, S>(f, d, n, u, F, p, out);
+                done = true;
+            }
+        }
+        if (!done) {
 #pragma unroll
-        for (int q = 0; q < Q; q++) collide_cell<L, S, MRT, Real, STRICT>(f, d, n, u, F, q, p, out[q]);
+            for (int q = 0; q < Q; q++) collide_cell<L, S, MRT, Real, STRICT>(f, d, n, u, F, q, p, out[q]);
+        }
         if constexpr (std::is_same<Real, float>::value) {
             Real rest = d;
 #pragma unroll

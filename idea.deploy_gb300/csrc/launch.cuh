@@ -30,6 +30,7 @@ struct HostSetup {
     const double *Beq;  // q*K
     bool a_nonzero;
     double omega;       // BGK rate (factored single-pass collision), 0 if not BGK
+    bool factored;      // FP64 BGK: the two-pass collision factored by opposite directions
     const double *w;    // q lattice weights
 };
 
@@ -126,6 +127,7 @@ struct Ops {
         p->neg_g = (Real)(-h.G);
         p->psi_kind = h.psi_kind;
         p->a_nonzero = h.a_nonzero ? 1 : 0;
+        p->factored = h.factored ? 1 : 0;
         for (int a = 0; a < S::QE; a++)
             for (int d = 0; d < D; d++)
                 p->sw[a][d] = (Real)((double)S::e(a, d) * h.we[a]);

@@ -917,6 +917,15 @@ int configure(sclbm_sim *s, int collision, double tau, const double *mrt_s, cons
     h.a_nonzero = a_nonzero;
     h.omega = (!mrt && !coll_a) ? (uniform_rate > 0 ? uniform_rate : 1.0 / tau) : 0.0;
     h.w = s->w.data();
+    // lattice weights symmetric under xi -> -xi and c2 = 1/3: what the factored form assumes
+    bool sym = std::fabs(s->c2 - 1.0 / 3.0) < 1e-12;
+    for (int q = 0; q < s->Q && sym; q++)
+        for (int k = 0; k < s->Q; k++) {
+            bool opp = true;
+            for (int d = 0; d < s->D; d++) opp = opp && s->xi[(size_t)q * s->D + d] == -s->xi[(size_t)k * s->D + d];
+            if (opp) sym = sym && s->w[q] == s->w[k];
+        }
+    h.factored = !s->fp32 && !mrt && h.omega > 0 && sym && s->literals == SCLBM_LIT_FACTORED;
     for (auto &g : s->graph)
         if (g) cudaGraphExecDestroy(g), g = nullptr;
     s->K = t.K;

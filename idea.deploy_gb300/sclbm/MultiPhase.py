@@ -14,8 +14,9 @@ Differences: every array lives in HBM behind one ``sclbm_sim`` handle (SoA,
 the reference's 'gpu' ordering); ``lang`` is accepted but there is one
 backend, with no CPU fallback.  Extra keywords: ``precision`` ('fp64' or
 'fp32_shifted'; ``fp32_flag=True`` selects the latter), ``rho0`` (shift of
-the FP32 storage), ``literals`` ('round15' as the reference prints them, or
-'exact'), ``collision_tables`` ((A, B) explicit operator, see include/sclbm.h),
+the FP32 storage), ``literals`` ('round15' as the reference prints them,
+'exact', or 'factored': exact, with the FP64 BGK operator factored by
+opposite directions), ``collision_tables`` ((A, B) explicit operator, see include/sclbm.h),
 ``noise_tables`` ((m2var, coef) explicit noise operator of the fluctuating step).
 
 Fluctuations (``fluctuations='Gross2011'`` with ``prng_kind``, ``init_seed``,
@@ -183,7 +184,7 @@ class ShanChenMultiPhase:
             psi_kind=self.psi_kind, collision=_lib.COLL_BGK, tau=p['tau'],
             precision=_lib.FP32_SHIFTED if precision == 'fp32_shifted' else _lib.FP64,
             rho0=float(p.get('rho0', 1.0)),
-            literals=_lib.LIT_EXACT if lit == 'exact' else _lib.LIT_ROUND15,
+            literals={'exact': _lib.LIT_EXACT, 'factored': _lib.LIT_FACTORED}.get(lit, _lib.LIT_ROUND15),
             device=int(p.get('device', 0) or 0),
             coll_a=None if tables is None else tables[0], coll_b=None if tables is None else tables[1])
         self._collision = ('tables',) if tables is not None else ('bgk', p['tau'])

@@ -16,7 +16,7 @@ PSI_EXP_INV, PSI_ONE_MINUS_EXP, PSI_IDENTITY = 0, 1, 2
 PATH_AUTO, PATH_TWO_PASS, PATH_FUSED, PATH_FUSED_PAIRS = 0, 1, 2, 3
 COLL_BGK, COLL_MRT = 0, 1
 FP64, FP32_SHIFTED = 0, 1
-LIT_ROUND15, LIT_EXACT = 0, 1
+LIT_ROUND15, LIT_EXACT, LIT_FACTORED = 0, 1, 2
 CRNG_NONE, CRNG_MINSTD, CRNG_NUMREC, CRNG_MMIX = 0, 1, 2, 3
 CRNG_KINDS = {'MINSTD': CRNG_MINSTD, 'NUMREC': CRNG_NUMREC, 'MMIX': CRNG_MMIX}
 SEEDS_STREAM_MAJOR, SEEDS_CELL_MAJOR = 0, 1

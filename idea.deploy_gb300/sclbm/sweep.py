@@ -209,8 +209,9 @@ def ragged_sweep(radii, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, che
 
 def plain_run(R, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, check_every=500, tol=1e-12,
               max_steps=200000, noise=0.0, seed=0, device=0, tol_dp=2e-5, patience=4, dim=2, L=None,
-              stop_at_dp=False):
-    """One droplet on the plain FP64 GPU path (exact coefficients), stopped by
+              stop_at_dp=False, literals=None):
+    """One droplet on the plain FP64 GPU path (exact coefficients; ``literals``
+    _lib.LIT_FACTORED factors the BGK operator as well), stopped by
     the reference's FP64 criterion u_conv < tol.  The step and wall time at
     which the FP32 batch's criterion (Laplace pressure calm to tol_dp for
     `patience` checks) would first have stopped it are recorded too; with
@@ -220,8 +221,8 @@ def plain_run(R, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, check_ever
     dims = (L,) * dim
     x, f = XIStencils['D2Q9' if dim == 2 else 'D3Q19'], FStencils[stencil]
     t0 = time.perf_counter()
-    s = _lib.Sim(dim, dims, x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], G, tau=tau, literals=_lib.LIT_EXACT,
-                 device=device)
+    s = _lib.Sim(dim, dims, x['XIs'], x['Ws'], x['c2'], f['Es'], f['Ws'], G, tau=tau,
+                 literals=_lib.LIT_EXACT if literals is None else literals, device=device)
     s.set_density(droplet(dims, R, rho_l, rho_g, width, seed, noise))
     s.set_velocity(np.zeros(dim * s.V))
     s.init_populations()
@@ -303,7 +304,7 @@ def laplace_fit(G=-4.5, radii=(12, 16, 20, 24, 32, 40, 48), stencil='D2E8', devi
 
 def run_sweep(n=64, r_min=8, seed=2024, G_range=(-6.0, -4.5), stencil='D2E8', check_every=500, tol_dp=2e-5,
               tol64=1e-12, max_steps=100000, coex_steps=200000, plain=True, device=0, init=None, mlp=None,
-              residual_max=0.1, plain_stop_at_dp=False):
+              residual_max=0.1, plain_stop_at_dp=False, plain_literals=None, plain_extra_literals=()):
     """The ragged droplet sweep: radii r_min .. r_min+n-1, box 4R rounded up to
     32, G uniform in G_range (seeded), densities from the flat-interface runs
     (from the thermodynamic construction where the slab diverged); batched
@@ -356,23 +357,30 @@ def run_sweep(n=64, r_min=8, seed=2024, G_range=(-6.0, -4.5), stencil='D2E8', ch
                coexistence_wall_s=t_coex, unstable=unstable, batch=sw, coexistence=coex, rho_l=rl, rho_g=rg,
                rho_source=source, warm=warm)
     if plain:
-        runs = []
-        t1 = time.perf_counter()
-        for i in range(n):
-            if sw['status'][i] == 'diverged':
-                runs.append(None)
-                continue
-            runs.append(plain_run(radii[i], float(Gs[i]), rl[i], rg[i], stencil=stencil, check_every=check_every,
-                                  tol=tol64, max_steps=max_steps, device=device, tol_dp=tol_dp,
-                                  stop_at_dp=plain_stop_at_dp))
-        res['plain'] = runs
-        res['plain_wall_s'] = time.perf_counter() - t1
+        # the plain FP64 arm (plain_literals: None = exact coefficients, or
+        # _lib.LIT_FACTORED), and optionally the same arm in other arithmetics
+        def arm(lit):
+            runs = []
+            t1 = time.perf_counter()
+            for i in range(n):
+                if sw['status'][i] == 'diverged':
+                    runs.append(None)
+                    continue
+                runs.append(plain_run(radii[i], float(Gs[i]), rl[i], rg[i], stencil=stencil, check_every=check_every,
+                                      tol=tol64, max_steps=max_steps, device=device, tol_dp=tol_dp,
+                                      stop_at_dp=plain_stop_at_dp, literals=lit))
+            return runs, time.perf_counter() - t1
+        res['plain'], res['plain_wall_s'] = arm(plain_literals)
+        res['plain_extra'] = {}
+        for lit in plain_extra_literals:
+            runs, wall = arm(lit)
+            res['plain_extra'][int(lit)] = dict(runs=runs, wall_s=wall)
     return res
 
 
 def run_sweep3d(n=256, seed=2025, R_range=(10.0, 30.0), G_range=(-6.0, -4.5), L=96, stencil='D3E6', check_every=500,
                 tol_dp=2e-5, tol64=1e-12, max_steps=20000, plain_sample=8, device=0, mlp=None, residual_max=None,
-                plain_stop_at_dp=False):
+                plain_stop_at_dp=False, plain_literals=None):
     """Batched 3D droplets: n D3Q19 droplets, radius and G uniform in their
     ranges (seeded), each in an L^3 periodic box, FP32-shifted batches (split
     so that Q * cells < 2^31 per batch); then the plain FP64 path, cold
@@ -426,7 +434,7 @@ def run_sweep3d(n=256, seed=2025, R_range=(10.0, 30.0), G_range=(-6.0, -4.5), L=
     for i in pick:
         r = plain_run(float(radii[i]), float(Gs[i]), rl[i], rg[i], stencil=stencil, check_every=check_every,
                       tol=tol64, max_steps=max_steps, device=device, dim=3, L=L, seed=seed + int(i),
-                      tol_dp=tol_dp, stop_at_dp=plain_stop_at_dp)
+                      tol_dp=tol_dp, stop_at_dp=plain_stop_at_dp, literals=plain_literals)
         r['index'] = int(i)
         plain.append(r)
     return dict(config=dict(n=n, seed=seed, R_range=list(R_range), G_range=list(G_range), box=L, stencil=stencil,

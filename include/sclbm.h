@@ -82,6 +82,10 @@ extern "C" {
 /* coefficient literals of the expanded collision */
 #define SCLBM_LIT_ROUND15 0        /* 15-significant-digit literals, as sympy evalf() emits */
 #define SCLBM_LIT_EXACT   1        /* exact coefficients rounded once to double */
+#define SCLBM_LIT_FACTORED 2       /* as EXACT; the FP64 BGK step also factors the operator
+                                      by opposite directions (fewer FP64 operations, equal up
+                                      to rounding; lattices with c2 = 1/3 and symmetric
+                                      weights); MRT takes EXACT */
 
 typedef struct sclbm_sim sclbm_sim;
 
