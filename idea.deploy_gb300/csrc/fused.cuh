@@ -869,7 +869,9 @@ struct BatchInst {
 // per SM (twelve 64-thread CTAs for BGK)
 constexpr int BATCH_TX_NARROW = 64;
 constexpr int batch_min_blocks(bool mrt, bool pairs, int nt) { return (mrt ? 512 : (pairs ? 1024 : 768)) / nt; }
-template <class L, class S, bool MRT, bool PAIRS = false, int TXB = 0>
+// ER: the compensated rest population (EXACT_REST of fused_tile); false only
+// for 3D paired batches whose caller trades it for speed
+template <class L, class S, bool MRT, bool PAIRS = false, int TXB = 0, bool ER = true>
 __global__ void __launch_bounds__(FusedShape<L, S, TXB>::NT,
                                   batch_min_blocks(MRT, PAIRS, FusedShape<L, S, TXB>::NT))
     k_fused_batch(const float *__restrict__ pop, float *__restrict__ pop_out,
@@ -896,7 +898,7 @@ __global__ void __launch_bounds__(FusedShape<L, S, TXB>::NT,
         const BatchInst I = inst[w.x];
         if (!I.active) continue;
         static_assert(TXB == 0 || L::D == 2, "narrow batch tiles: 2D");
-        fused_tile<L, S, MRT, void, false, PAIRS, 0, TXB, 0, true>(pop + I.base, pop_out + I.base, Vtot, I.Lx, I.Ly,
+        fused_tile<L, S, MRT, void, false, PAIRS, 0, TXB, 0, ER>(pop + I.base, pop_out + I.base, Vtot, I.Lx, I.Ly,
                                                                  I.Lz, w.y, w.z,
                                                   w.w & 0xffff, w.w >> 16, I.neg_g, I.rho0, p, smem);
     }

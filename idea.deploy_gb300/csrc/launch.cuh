@@ -64,9 +64,10 @@ struct KernelOps {
     int fused_tile_mask; // kTiles shapes built (bit t) for the paired single pass (bit 0: the default)
     // batches of lattices (FP32 only, else null)
     // tx: tile width of a 2D batch (0: fused_tx; BATCH_TX_NARROW: the narrow tiles)
+    // exact_rest 0 (3D paired BGK only): the rest population without the compensated sums
     cudaError_t (*batch_step)(const void *pop, void *pop_out, const void *sp, const BatchInst *inst, const int4 *items,
-                              int n_items, int Vtot, int *counter, int parity, int pairs, int tx, int grid,
-                              cudaStream_t st);
+                              int n_items, int Vtot, int *counter, int parity, int pairs, int tx, int exact_rest,
+                              int grid, cudaStream_t st);
     int (*batch_occupancy)(int pairs, int tx);  // resident CTAs per SM of the batch kernel
     cudaError_t (*batch_density)(const void *pop, void *dn, void *psi, const void *sp, const BatchInst *inst, int n_inst,
                                  int Vtot, int gx, cudaStream_t st);
@@ -334,24 +335,24 @@ struct Ops {
         }
         return 0;
     }
-    template <bool PAIRS, int TXB>
+    template <bool PAIRS, int TXB, bool ER = true>
     static void batch_allow_smem() {
         using SH = FusedShape<L, S, TXB>;
         static bool done[64] = {};
         int dev = 0;
         cudaGetDevice(&dev);
         if (dev < 0 || dev >= 64 || !done[dev]) {
-            cudaFuncSetAttribute(k_fused_batch<L, S, MRT, PAIRS, TXB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 SH::SMEM);
+            cudaFuncSetAttribute(k_fused_batch<L, S, MRT, PAIRS, TXB, ER>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, SH::SMEM);
             if (dev >= 0 && dev < 64) done[dev] = true;
         }
     }
-    template <bool PAIRS, int TXB>
+    template <bool PAIRS, int TXB, bool ER = true>
     static cudaError_t batch_launch(const void *pop, void *pop_out, const void *sp, const BatchInst *inst,
                                     const int4 *items, int n_items, int Vtot, int *counter, int parity, int grid,
                                     cudaStream_t st) {
         using SH = FusedShape<L, S, TXB>;
-        batch_allow_smem<PAIRS, TXB>();
+        batch_allow_smem<PAIRS, TXB, ER>();
         // programmatic dependent launch: a step's CTAs are placed while the
         // previous step's last items finish, and wait (griddepcontrol.wait)
         // for its completion before they read anything
@@ -365,13 +366,19 @@ struct Ops {
         at[0].val.programmaticStreamSerializationAllowed = 1;
         cfg.attrs = at;
         cfg.numAttrs = 1;
-        return cudaLaunchKernelEx(&cfg, k_fused_batch<L, S, MRT, PAIRS, TXB>, (const float *)pop, (float *)pop_out,
+        return cudaLaunchKernelEx(&cfg, k_fused_batch<L, S, MRT, PAIRS, TXB, ER>, (const float *)pop, (float *)pop_out,
                                   *static_cast<const SP *>(sp), inst, items, n_items, Vtot, counter, parity);
     }
     static cudaError_t batch_step(const void *pop, void *pop_out, const void *sp, const BatchInst *inst,
                                   const int4 *items, int n_items, int Vtot, int *counter, int parity, int pairs,
-                                  int tx, int grid, cudaStream_t st) {
+                                  int tx, int exact_rest, int grid, cudaStream_t st) {
         if constexpr (std::is_same<Real, float>::value) {
+            if constexpr (L::D == 3 && S::R % 2 == 0 && !MRT) {
+                if (pairs && !exact_rest)
+                    return batch_launch<true, 0, false>(pop, pop_out, sp, inst, items, n_items, Vtot, counter, parity,
+                                                        grid, st);
+            }
+            if (!exact_rest) return cudaErrorNotSupported;
             if constexpr (L::D == 3 && S::R % 2 == 0) {
                 if (pairs)
                     return batch_launch<true, 0>(pop, pop_out, sp, inst, items, n_items, Vtot, counter, parity, grid,

@@ -1914,6 +1914,7 @@ struct sclbm_batch {
     int gx = 1, grid = 1, chunk = 32;
     int pairs = 0;          // 3D, even radius, every Lx and first cell even: paired halo loads
     int tx = 0;             // 2D tile width (0: the single-lattice kernel's; BATCH_TX_NARROW)
+    int exact_rest = 1;     // compensated rest population (0: 3D paired BGK batches only)
     std::vector<int> home;  // buffer holding a retired lattice's state (-1 while active)
     std::vector<int64_t> steps;
     bool pop_set = false;
@@ -2013,7 +2014,7 @@ int batch_plan(sclbm_batch *b) {
 
 int batch_launch_step(sclbm_batch *b) {
     cudaError_t e = b->ops->batch_step(b->pop[b->cur], b->pop[b->cur ^ 1], b->sp.data(), b->inst_d, b->items_d,
-                                       (int)b->items.size(), (int)b->Vtot, b->counter, b->cur, b->pairs, b->tx, b->grid,
+                                       (int)b->items.size(), (int)b->Vtot, b->counter, b->cur, b->pairs, b->tx, b->exact_rest, b->grid,
                                        b->st);
     if (e != cudaSuccess) return fail(SCLBM_ERR_CUDA, "batch step: %s", cudaGetErrorString(e));
     b->cur ^= 1;
@@ -2402,6 +2403,16 @@ int sclbm_batch_set_tile_width(sclbm_batch *b, int tx) {
     DevGuard dg(b->device);
     b->tx = tx;
     return batch_plan(b);
+}
+
+int sclbm_batch_set_mass_compensation(sclbm_batch *b, int on) {
+    if (!b) return fail(SCLBM_ERR_ARG, "null handle");
+    if (!on && !b->pairs)
+        return fail(SCLBM_ERR_UNSUPPORTED, "the uncompensated step is built for 3D batches with paired halo loads only");
+    b->exact_rest = on ? 1 : 0;
+    for (auto &g : b->graph)
+        if (g) cudaGraphExecDestroy(g), g = nullptr;  // they hold the kernel
+    return SCLBM_OK;
 }
 
 int sclbm_batch_set_probe_radius(sclbm_batch *b, int rad) {

@@ -108,6 +108,7 @@ SIGNATURES = {
     'sclbm_batch_probe': [_P, _P, _P],
     'sclbm_batch_set_probe_radius': [_P, ctypes.c_int],
     'sclbm_batch_set_tile_width': [_P, ctypes.c_int],
+    'sclbm_batch_set_mass_compensation': [_P, ctypes.c_int],
     'sclbm_selftest_bounded_wait': [ctypes.c_int, ctypes.c_int, ctypes.POINTER(ctypes.c_int),
                                     ctypes.POINTER(ctypes.c_double)],
     'sclbm_restore_mass': [_P, _D, _DP],

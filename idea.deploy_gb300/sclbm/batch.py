@@ -116,6 +116,11 @@ class Batch:
         """2D batches: 0 (256-cell tiles, the default) or 64; bit-identical results."""
         _lib.call('sclbm_batch_set_tile_width', self.h, int(tx))
 
+    def set_mass_compensation(self, on):
+        """Compensated rest population (default on); off only for 3D batches
+        with paired halo loads."""
+        _lib.call('sclbm_batch_set_mass_compensation', self.h, int(bool(on)))
+
     def set_probe_radius(self, rad):
         """probe() returns means over the cube of side 2 rad + 1 about each cell."""
         _lib.call('sclbm_batch_set_probe_radius', self.h, int(rad))

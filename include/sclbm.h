@@ -407,6 +407,14 @@ SCLBM_API int sclbm_batch_set_probe_radius(sclbm_batch *b, int rad);
  * 256-cell rows).  The results are bit-identical.  3D batches take 0 only.
  * No counterpart in the reference. */
 SCLBM_API int sclbm_batch_set_tile_width(sclbm_batch *b, int tx);
+/* on (the default): each cell's rest population absorbs the rounding errors
+ * of its density sum and of the subtraction chain (compensated sums), so the
+ * stored FP32 populations conserve mass to one rounding per cell and step;
+ * off: plain FP32 sums, ~11 % shorter steps, mass drift left to
+ * sclbm_batch_restore_mass.  Off is built for 3D batches with paired halo
+ * loads only (SCLBM_ERR_UNSUPPORTED otherwise).  No counterpart in the
+ * reference. */
+SCLBM_API int sclbm_batch_set_mass_compensation(sclbm_batch *b, int on);
 
 /* ---------------------------------------------------------------------------
  * Warm-start surrogate: an MLP 5 -> 64 -> 64 -> 64 -> 1 with SiLU, BF16

@@ -112,6 +112,36 @@ def test_narrow_2d_tiles_bit_identical(st):
         assert np.array_equal(out[0][i], out[1][i]), i
 
 
+def test_mass_compensation_off():
+    """Plain FP32 sums for the rest population (3D paired batches): the same
+    step up to FP32 rounding; refused where it is not built."""
+    lat, st, dims, G, rho0 = CASES['3d']
+    n0 = densities(dims)
+    out, mass = [], []
+    for on in (True, False):
+        b = Batch(XIStencils[lat], FStencils[st], dims, G, rho0)
+        b.set_mass_compensation(on)
+        for i, n in enumerate(n0):
+            b.set_density(i, n)
+        b.init_populations()
+        m0 = b.restore_mass()
+        b.step(60)
+        mass.append(b.restore_mass() / m0 - 1)
+        out.append([b.get_density(i) for i in range(len(dims))])
+        b.close()
+    for i in range(len(dims)):
+        assert rel_err(out[1][i], out[0][i]) < 1e-5, i
+    # compensated: one FP32 rounding of the rest population per cell and step
+    # (~1e-9 after 60 steps); plain sums drift two orders of magnitude more
+    assert np.abs(mass[0]).max() < 1e-8 and np.abs(mass[1]).max() < 1e-5, mass
+    assert np.abs(mass[1]).max() > 10 * np.abs(mass[0]).max(), mass
+    lat, st, dims, G, rho0 = CASES['2d']
+    b = Batch(XIStencils[lat], FStencils[st], dims, G, rho0)
+    with pytest.raises(_lib.SclbmError):
+        b.set_mass_compensation(False)
+    b.close()
+
+
 def test_narrow_tiles_refused_in_3d():
     lat, st, dims, G, rho0 = CASES['3d']
     b = Batch(XIStencils[lat], FStencils[st], dims, G, rho0)
