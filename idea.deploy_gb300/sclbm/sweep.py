@@ -152,8 +152,10 @@ def ragged_sweep(radii, G, rho_l, rho_g, stencil='D2E8', tau=1.0, width=2.0, che
     if not (compensate if compensate is not None else dim == 2):
         try:
             b.set_mass_compensation(False)
-        except _lib.SclbmError:
-            pass  # built for 3D batches with paired halo loads only: the others keep it
+        except _lib.SclbmError as e:
+            # built for 3D batches with paired halo loads only: the others keep it
+            if e.status != _lib.ERR_UNSUPPORTED:
+                raise
     for i in range(n):
         b.set_density(i, init[i] if init is not None else cold(i))
     b.init_populations()
